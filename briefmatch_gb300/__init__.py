@@ -1,0 +1,352 @@
+"""briefmatch_gb300 -- GB300-native BriefMatch dense optical flow.
+
+Python view of the engine's C ABI (include/briefmatch_gb300.h), loaded with
+ctypes from the in-tree library briefmatch_gb300/_lib/libbriefmatch_gb300.so.
+There is no CPU fallback: importing the engine without its compiled library
+raises.  Device buffers handed to the stage functions are raw CUDA pointers
+(for example ``tensor.data_ptr()`` of a torch CUDA tensor).
+
+The classes mirror the reference's host API:
+  BMParams    briefmatch.h:65-89
+  BriefMatch  briefmatch.h:108-155 (setup/match/downsample/process/swap/convert)
+  FlowEngine  OFPipeline::processFrame (of_pipeline.cpp:241-387) over 8-bit frames
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libbriefmatch_gb300.so")
+
+BM_PATCH_MAX = 2048
+BM_MAX_MEDIAN = 47
+BM_CONST_KERNEL_SIZE = 100
+
+BM_OK, BM_ERR_INVALID, BM_ERR_LIMIT, BM_ERR_CUDA, BM_ERR_STATE, BM_ERR_NOMEM, BM_ERR_TIMEOUT, BM_ERR_IO = range(8)
+BM_RNG_XORWOW, BM_RNG_PHILOX = 0, 1
+(BM_BUF_FEAT1, BM_BUF_FEAT2, BM_BUF_FLOW, BM_BUF_COST, BM_BUF_UP, BM_BUF_FLOW_IN, BM_BUF_FLOW_MED,
+ BM_BUF_FLOW_OUT, BM_BUF_FRAME, BM_BUF_FRAME_PREV) = range(10)
+
+
+class BriefMatchException(RuntimeError):
+    """Parameter-limit and state errors (briefmatch.h:91-106)."""
+
+
+class CudaException(RuntimeError):
+    """CUDA runtime errors (util_cuda.h:85-100)."""
+
+
+class bm_params(ctypes.Structure):
+    _fields_ = [
+        ("sx", ctypes.c_uint32), ("sy", ctypes.c_uint32), ("sx_in", ctypes.c_uint32), ("sy_in", ctypes.c_uint32),
+        ("N", ctypes.c_uint32), ("iterations", ctypes.c_uint32), ("jfMax", ctypes.c_uint32), ("P", ctypes.c_uint32),
+        ("fsize", ctypes.c_uint32),
+        ("patchArea", ctypes.c_float), ("sigma", ctypes.c_float), ("sEPE", ctypes.c_float), ("sI", ctypes.c_float),
+        ("sS", ctypes.c_float), ("maxmot", ctypes.c_float),
+        ("doubleProp", ctypes.c_int32), ("filter", ctypes.c_int32), ("tInit", ctypes.c_int32),
+        ("rng", ctypes.c_uint32), ("seed", ctypes.c_uint64),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_lib = None
+
+
+def _declare(lib):
+    P = ctypes.POINTER
+    c = ctypes
+    sig = {
+        "bm_params_default": (c.c_int, [P(bm_params)]),
+        "bm_params_derive": (c.c_int, [P(bm_params), c.c_uint32, c.c_uint32, c.c_float, c.c_float, c.c_float,
+                                       c.c_float, c.c_float, c.c_float]),
+        "bm_make_pattern": (c.c_int, [P(bm_params), c.c_uint64, P(c.c_float)]),
+        "bm_gauss_taps": (c.c_int, [c.c_float, P(c.c_float), P(c.c_uint32)]),
+        "bm_create": (c.c_int, [P(bm_params), P(c.c_void_p)]),
+        "bm_destroy": (c.c_int, [c.c_void_p]),
+        "bm_get_params": (c.c_int, [c.c_void_p, P(bm_params)]),
+        "bm_set_stream": (c.c_int, [c.c_void_p, c.c_void_p]),
+        "bm_synchronize": (c.c_int, [c.c_void_p]),
+        "bm_set_pattern": (c.c_int, [c.c_void_p, P(c.c_float), c.c_uint32]),
+        "bm_buffer": (c.c_int, [c.c_void_p, c.c_int, P(c.c_void_p), P(c.c_size_t)]),
+        "bm_feature_stride": (c.c_uint32, [c.c_void_p]),
+        "bm_read_buffer": (c.c_int, [c.c_void_p, c.c_int, c.c_void_p, c.c_size_t, c.c_int]),
+        "bm_write_buffer": (c.c_int, [c.c_void_p, c.c_int, c.c_void_p, c.c_size_t, c.c_int]),
+        "bm_upsample": (c.c_int, [c.c_void_p, c.c_void_p, c.c_void_p]),
+        "bm_upsample_u8": (c.c_int, [c.c_void_p, c.c_void_p, c.c_void_p]),
+        "bm_features": (c.c_int, [c.c_void_p, c.c_void_p, c.c_int]),
+        "bm_initialize": (c.c_int, [c.c_void_p, c.c_int]),
+        "bm_propagate": (c.c_int, [c.c_void_p, c.c_int]),
+        "bm_random_search": (c.c_int, [c.c_void_p]),
+        "bm_match": (c.c_int, [c.c_void_p, c.c_void_p, c.c_void_p]),
+        "bm_downsample": (c.c_int, [c.c_void_p]),
+        "bm_process": (c.c_int, [c.c_void_p, c.c_void_p]),
+        "bm_swap": (c.c_int, [c.c_void_p]),
+        "bm_convert": (c.c_int, [c.c_void_p, c.c_void_p, c.c_void_p]),
+        "bm_export_field": (c.c_int, [c.c_void_p, c.c_void_p, c.c_void_p, c.c_void_p]),
+        "bm_import_field": (c.c_int, [c.c_void_p, c.c_void_p, c.c_void_p, c.c_void_p]),
+        "bm_normals": (c.c_int, [c.c_void_p, c.c_uint64, c.c_void_p]),
+        "bm_nn_indices": (c.c_int, [c.c_void_p, c.c_void_p, c.c_void_p]),
+        "bm_rng_position": (c.c_int, [c.c_void_p, P(c.c_uint64)]),
+        "bm_set_rng_position": (c.c_int, [c.c_void_p, c.c_uint64]),
+        "bm_frame": (c.c_int, [c.c_void_p, c.c_void_p, c.c_int, c.c_void_p, c.c_void_p, c.c_int]),
+        "bm_reset_sequence": (c.c_int, [c.c_void_p]),
+        "bm_launch_count": (c.c_uint64, [c.c_void_p]),
+        "bm_last_error": (c.c_char_p, []),
+        "bm_version": (c.c_char_p, []),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    return lib
+
+
+def lib():
+    """The engine library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(
+                "briefmatch_gb300: engine library missing at %s; run __graft_entry__.build() "
+                "(the engine has no CPU fallback)" % LIB_PATH)
+        _lib = _declare(ctypes.CDLL(LIB_PATH))
+    return _lib
+
+
+def check(status):
+    if status == BM_OK:
+        return
+    msg = lib().bm_last_error().decode(errors="replace")
+    if status in (BM_ERR_LIMIT, BM_ERR_STATE, BM_ERR_INVALID):
+        raise BriefMatchException(msg)
+    raise CudaException("status %d: %s" % (status, msg))
+
+
+def _fptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+class BMParams:
+    """BMParams (briefmatch.h:65-89) with OFPipeline's derivation (of_pipeline.cpp:178-190)."""
+
+    def __init__(self, **kw):
+        self._p = bm_params()
+        check(lib().bm_params_default(ctypes.byref(self._p)))
+        for k, v in kw.items():
+            setattr(self._p, k, v)
+
+    @classmethod
+    def derive(cls, width, height, ux=0.0, uy=0.0, patch_radius=3.0, sigma_downsampling=0.025, median_size=1.0,
+               range_spatial=0.85, **kw):
+        """Parameters for a width x height input as OFPipeline::setParams derives them
+        from the command-line percentages (defaults of_pipeline.cpp:94-95)."""
+        self = cls(**kw)
+        check(lib().bm_params_derive(ctypes.byref(self._p), width, height, ux, uy, patch_radius, sigma_downsampling,
+                                     median_size, range_spatial))
+        return self
+
+    def __getattr__(self, k):
+        if k.startswith("_"):
+            raise AttributeError(k)
+        return getattr(self._p, k)
+
+    def __setattr__(self, k, v):
+        if k == "_p":
+            object.__setattr__(self, k, v)
+        else:
+            setattr(self._p, k, v)
+
+    def struct(self):
+        return self._p
+
+    def as_dict(self):
+        return self._p.as_dict()
+
+    def make_pattern(self, seed=0):
+        out = np.zeros(4 * self._p.N, np.float32)
+        check(lib().bm_make_pattern(ctypes.byref(self._p), seed, _fptr(out)))
+        return out
+
+    def gauss_taps(self):
+        out = np.zeros(BM_CONST_KERNEL_SIZE, np.float32)
+        P = ctypes.c_uint32(0)
+        check(lib().bm_gauss_taps(self._p.sigma, _fptr(out), ctypes.byref(P)))
+        return out[: P.value].copy()
+
+    def search_dist(self):
+        """Random-search radius, briefmatch.cpp:271."""
+        return float(np.sqrt(np.ceil(np.float32(self._p.sx) * np.float32(0.5) / np.float32(3.0)), dtype=np.float32))
+
+
+class BriefMatch:
+    """Engine context over the C ABI; method names follow briefmatch.h:108-135."""
+
+    def __init__(self, params: BMParams | None = None):
+        self.params = params or BMParams()
+        self._ctx = ctypes.c_void_p(None)
+
+    # lifecycle -------------------------------------------------------------
+    def setup(self):
+        if self._ctx:
+            return
+        check(lib().bm_create(ctypes.byref(self.params.struct()), ctypes.byref(self._ctx)))
+        p = bm_params()
+        check(lib().bm_get_params(self._ctx, ctypes.byref(p)))
+        self.params.P = p.P
+
+    def clean(self):
+        if self._ctx:
+            lib().bm_destroy(self._ctx)
+            self._ctx = ctypes.c_void_p(None)
+
+    def __del__(self):
+        try:
+            self.clean()
+        except Exception:
+            pass
+
+    def isSetup(self):
+        return bool(self._ctx)
+
+    @property
+    def ctx(self):
+        if not self._ctx:
+            raise BriefMatchException("BriefMatch is not initialized before use.")
+        return self._ctx
+
+    # configuration -------------------------------------------------------------
+    def set_stream(self, stream_ptr):
+        check(lib().bm_set_stream(self.ctx, ctypes.c_void_p(stream_ptr)))
+
+    def synchronize(self):
+        check(lib().bm_synchronize(self.ctx))
+
+    def set_pattern(self, pattern):
+        pat = np.ascontiguousarray(pattern, dtype=np.float32)
+        check(lib().bm_set_pattern(self.ctx, _fptr(pat), pat.size))
+
+    def buffer(self, which):
+        ptr = ctypes.c_void_p(None)
+        nbytes = ctypes.c_size_t(0)
+        check(lib().bm_buffer(self.ctx, which, ctypes.byref(ptr), ctypes.byref(nbytes)))
+        return ptr.value, nbytes.value
+
+    def read_buffer(self, which, dtype, count=None):
+        """Host copy of a context buffer as a numpy array."""
+        _, nbytes = self.buffer(which)
+        dt = np.dtype(dtype)
+        count = nbytes // dt.itemsize if count is None else count
+        out = np.empty(count, dt)
+        check(lib().bm_read_buffer(self.ctx, which, out.ctypes.data, out.nbytes, 0))
+        return out
+
+    def write_buffer(self, which, array):
+        a = np.ascontiguousarray(array)
+        check(lib().bm_write_buffer(self.ctx, which, a.ctypes.data, a.nbytes, 0))
+
+    def feature_stride(self):
+        return lib().bm_feature_stride(self.ctx)
+
+    # stages ---------------------------------------------------------------
+    def upsample(self, d_in, d_out):
+        check(lib().bm_upsample(self.ctx, ctypes.c_void_p(d_in), ctypes.c_void_p(d_out)))
+
+    def upsample_u8(self, d_in, d_out):
+        check(lib().bm_upsample_u8(self.ctx, ctypes.c_void_p(d_in), ctypes.c_void_p(d_out)))
+
+    def features(self, d_up, slot):
+        check(lib().bm_features(self.ctx, ctypes.c_void_p(d_up), slot))
+
+    def initialize(self, first):
+        check(lib().bm_initialize(self.ctx, int(bool(first))))
+
+    def propagate(self, pd):
+        check(lib().bm_propagate(self.ctx, pd))
+
+    def random_search(self):
+        check(lib().bm_random_search(self.ctx))
+
+    def match(self, d_im1, d_im2):
+        check(lib().bm_match(self.ctx, ctypes.c_void_p(d_im1 or 0), ctypes.c_void_p(d_im2)))
+
+    def downsample(self):
+        check(lib().bm_downsample(self.ctx))
+
+    def process(self, d_prev_in):
+        check(lib().bm_process(self.ctx, ctypes.c_void_p(d_prev_in)))
+
+    def swap(self):
+        check(lib().bm_swap(self.ctx))
+
+    def convert(self):
+        n = self.params.sx_in * self.params.sy_in
+        u = np.empty(n, np.float32)
+        v = np.empty(n, np.float32)
+        check(lib().bm_convert(self.ctx, u.ctypes.data, v.ctypes.data))
+        return u.reshape(self.params.sy_in, self.params.sx_in), v.reshape(self.params.sy_in, self.params.sx_in)
+
+    def export_field(self, d_nx, d_ny, d_dist):
+        check(lib().bm_export_field(self.ctx, ctypes.c_void_p(d_nx or 0), ctypes.c_void_p(d_ny or 0),
+                                    ctypes.c_void_p(d_dist or 0)))
+
+    def import_field(self, d_nx, d_ny, d_cost):
+        check(lib().bm_import_field(self.ctx, ctypes.c_void_p(d_nx), ctypes.c_void_p(d_ny),
+                                    ctypes.c_void_p(d_cost or 0)))
+
+    def normals(self, call, d_out):
+        check(lib().bm_normals(self.ctx, call, ctypes.c_void_p(d_out)))
+
+    def nn_indices(self):
+        """resizeNN source column/row per input column/row (util_cuda.cu:165-166)."""
+        xs = np.empty(self.params.sx_in, np.uint32)
+        ys = np.empty(self.params.sy_in, np.uint32)
+        check(lib().bm_nn_indices(self.ctx, xs.ctypes.data, ys.ctypes.data))
+        return xs, ys
+
+    def rng_position(self):
+        v = ctypes.c_uint64(0)
+        check(lib().bm_rng_position(self.ctx, ctypes.byref(v)))
+        return v.value
+
+    def set_rng_position(self, calls):
+        check(lib().bm_set_rng_position(self.ctx, calls))
+
+    def frame(self, frame_ptr, on_device, u_ptr=None, v_ptr=None, out_on_device=True):
+        check(lib().bm_frame(self.ctx, ctypes.c_void_p(frame_ptr), int(bool(on_device)), ctypes.c_void_p(u_ptr or 0),
+                             ctypes.c_void_p(v_ptr or 0), int(bool(out_on_device))))
+
+    def reset_sequence(self):
+        check(lib().bm_reset_sequence(self.ctx))
+
+    def launch_count(self):
+        return int(lib().bm_launch_count(self.ctx))
+
+
+class FlowEngine(BriefMatch):
+    """Frame-at-a-time flow over 8-bit host frames: OFPipeline::processFrame
+    (of_pipeline.cpp:241-387) without file I/O.  The first frame primes the
+    context and yields zeros; each later frame yields the flow from the previous
+    frame to it, sampled on the previous frame's grid, as (u, v) float32 arrays."""
+
+    def __init__(self, params: BMParams):
+        super().__init__(params)
+        self.setup()
+
+    def process_frame(self, frame_u8):
+        f = np.ascontiguousarray(frame_u8, dtype=np.uint8)
+        p = self.params
+        if f.shape != (p.sy_in, p.sx_in):
+            raise BriefMatchException("frame shape %s does not match %dx%d" % (f.shape, p.sx_in, p.sy_in))
+        u = np.empty((p.sy_in, p.sx_in), np.float32)
+        v = np.empty((p.sy_in, p.sx_in), np.float32)
+        self.frame(f.ctypes.data, False, u.ctypes.data, v.ctypes.data, out_on_device=False)
+        return u, v
+
+
+def version():
+    return lib().bm_version().decode()

@@ -1,0 +1,660 @@
+// bm_api.cu -- the C ABI of the engine: context (buffer ownership as in
+// BriefMatch::setup, briefmatch.cpp:72-214), the stage entry points that stand in
+// for the reference's CUDA_* launchers, and the one-frame pipeline of
+// OFPipeline::processFrame (of_pipeline.cpp:241-333).
+//
+// Nothing here synchronises the device except calls that hand data back to the
+// host; the reference synchronises after every launch (util_cuda.cu:185-275).
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "bm_internal.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+bm_status fail(bm_status st, const char* fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return st;
+}
+
+#define BM_CUDA(call)                                                                        \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess)                                                               \
+            return fail(BM_ERR_CUDA, "%s in %s at line %d", cudaGetErrorString(e_), __FILE__, \
+                        __LINE__);                                                           \
+    } while (0)
+
+#define BM_LAUNCH(ctx, call)   \
+    do {                       \
+        BM_CUDA(call);         \
+        (ctx)->launches++;     \
+    } while (0)
+
+}  // namespace
+
+struct bm_ctx {
+    bm_params prm;
+    uint32_t nsp = 1;
+    size_t npix = 0, npix_in = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+
+    uint8_t* d_frame_u8 = nullptr;
+    float* d_frame[2] = {nullptr, nullptr};  // [cur_frame] current, [cur_frame^1] previous
+    int cur_frame = 0;
+    float* d_up = nullptr;
+    uint32_t* d_feat[2] = {nullptr, nullptr};
+    int feat1 = 0;                           // d_feat[feat1] is FEAT1, d_feat[feat1^1] FEAT2
+    uint32_t* d_flow[2] = {nullptr, nullptr};
+    int flow_cur = 0;
+    uint16_t* d_cost = nullptr;
+    float* d_flow_in = nullptr;    // U then V, npix_in each
+    float* d_flow_med = nullptr;
+    float* d_flow_out = nullptr;
+    float* d_tmp = nullptr;
+    int4* d_pattern = nullptr;
+    int pattern_rmax = 0;
+    float* d_taps = nullptr;
+    float* d_lx = nullptr;
+    int* d_ix = nullptr;
+    float* d_ly = nullptr;
+    int* d_iy = nullptr;
+    unsigned int* d_nnx = nullptr;   // resizeNN source column per input column
+    unsigned int* d_nny = nullptr;   // resizeNN source row per input row
+
+    float dist = 0;          // random-search radius, briefmatch.cpp:271
+    int tri_s = 0;           // trilateral half window, briefmatch_cuda.cu:266
+    uint64_t rs_calls = 0;   // random-search calls made so far
+    bool first_match = true; // BriefMatch::m_firstFrame
+    bool primed = false;
+    uint64_t launches = 0;
+
+    uint32_t* feat1_ptr() const { return d_feat[feat1]; }
+    uint32_t* feat2_ptr() const { return d_feat[feat1 ^ 1]; }
+};
+
+namespace {
+
+template <typename T>
+bm_status dev_alloc(T** p, size_t count)
+{
+    *p = nullptr;
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return fail(BM_ERR_NOMEM, "cudaMalloc of %zu bytes failed: %s", count * sizeof(T), cudaGetErrorString(e));
+    }
+    return BM_OK;
+}
+
+void release(bm_ctx* c)
+{
+    void* ptrs[] = {c->d_frame_u8, c->d_frame[0], c->d_frame[1], c->d_up, c->d_feat[0], c->d_feat[1],
+                    c->d_flow[0], c->d_flow[1], c->d_cost, c->d_flow_in, c->d_flow_med, c->d_flow_out,
+                    c->d_tmp, c->d_pattern, c->d_taps, c->d_lx, c->d_ix, c->d_ly, c->d_iy,
+                    c->d_nnx, c->d_nny};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (c->own_stream) cudaStreamDestroy(c->own_stream);
+}
+
+bm_status check_ctx(const bm_ctx* c)
+{
+    if (!c) return fail(BM_ERR_INVALID, "null context");
+    return BM_OK;
+}
+
+bmk::RsArgs rs_args(const bm_ctx* c, bool enabled)
+{
+    bmk::RsArgs rs;
+    rs.enabled = enabled ? 1 : 0;
+    rs.mode = (int)c->prm.rng;
+    rs.seed = c->prm.seed;
+    rs.call = c->rs_calls;
+    rs.dist = c->dist;
+    return rs;
+}
+
+bm_status features_into(bm_ctx* c, const float* d_up, uint32_t* F)
+{
+    const bm_params& p = c->prm;
+    BM_LAUNCH(c, bmk::features(d_up, F, (int)p.sx, (int)p.sy, (int)p.N, (int)c->nsp, c->d_pattern, c->pattern_rmax,
+                               c->stream));
+    return BM_OK;
+}
+
+// One jump-flood pass; the random search of this iteration is fused into the last
+// level when fuse_rs is set (it reads only the pixel's own state).
+bm_status propagate_pass(bm_ctx* c, int pd, bool fuse_rs)
+{
+    const bm_params& p = c->prm;
+    int levels = 0;
+    for (int step = (int)p.jfMax; step > 0; step /= 2) levels++;
+    int lvl = 0;
+    for (int step = (int)p.jfMax; step > 0; step /= 2, lvl++) {
+        const bool last = (lvl == levels - 1);
+        bmk::RsArgs rs = rs_args(c, fuse_rs && last);
+        BM_LAUNCH(c, bmk::jump_level(c->feat1_ptr(), c->feat2_ptr(), c->d_flow[c->flow_cur], c->d_flow[c->flow_cur ^ 1],
+                                     c->d_cost, (int)p.sx, (int)p.sy, (int)c->nsp, step, pd, p.doubleProp ? 1 : 0, rs,
+                                     c->stream));
+        c->flow_cur ^= 1;
+    }
+    if (fuse_rs) {
+        if (levels == 0) {
+            bmk::RsArgs rs = rs_args(c, true);
+            BM_LAUNCH(c, bmk::random_search(c->feat1_ptr(), c->feat2_ptr(), c->d_flow[c->flow_cur], c->d_cost, (int)p.sx,
+                                            (int)p.sy, (int)c->nsp, rs, c->stream));
+        }
+        c->rs_calls++;
+    }
+    return BM_OK;
+}
+
+bm_status match_impl(bm_ctx* c, const float* d_im2)
+{
+    const bm_params& p = c->prm;
+    bm_status st = features_into(c, d_im2, c->feat2_ptr());
+    if (st != BM_OK) return st;
+    const int first = (c->first_match || !p.tInit) ? 1 : 0;
+    BM_LAUNCH(c, bmk::initialize(c->feat1_ptr(), c->feat2_ptr(), c->d_flow[c->flow_cur], c->d_flow[c->flow_cur ^ 1],
+                                 c->d_cost, (int)p.sx, (int)p.sy, (int)c->nsp, first, c->stream));
+    c->flow_cur ^= 1;
+    int pd = -1;
+    for (uint32_t it = 0; it < p.iterations; it++) {
+        st = propagate_pass(c, pd, true);
+        if (st != BM_OK) return st;
+        pd = -pd;
+    }
+    c->first_match = false;
+    return BM_OK;
+}
+
+bm_status downsample_impl(bm_ctx* c)
+{
+    const bm_params& p = c->prm;
+    float* U = c->d_flow_in;
+    float* V = c->d_flow_in + c->npix_in;
+    if (p.sx_in != p.sx || p.sy_in != p.sy) {
+        const float mx = (float)p.sx_in / (float)p.sx;  // briefmatch.cpp:316-317
+        const float my = (float)p.sy_in / (float)p.sy;
+        BM_LAUNCH(c, bmk::downsample(c->d_flow[c->flow_cur], U, V, (int)p.sx, (int)p.sy, (int)p.sx_in, (int)p.sy_in,
+                                     c->d_taps, (int)p.P, mx, my, c->d_nnx, c->d_nny, c->stream));
+    } else {
+        // briefmatch.cpp:319-323: the converted field is the output
+        BM_LAUNCH(c, bmk::flow_to_planes(c->d_flow[c->flow_cur], U, V, c->npix, c->stream));
+    }
+    return BM_OK;
+}
+
+bm_status process_impl(bm_ctx* c, const float* d_prev_in)
+{
+    const bm_params& p = c->prm;
+    const size_t n = c->npix_in;
+    float* U = c->d_flow_in;
+    float* V = U + n;
+    if (p.filter) {
+        if (!d_prev_in) return fail(BM_ERR_INVALID, "process: the guide frame is required when filtering");
+        const int fs = p.fsize == 0 ? 1 : (int)p.fsize;
+        BM_LAUNCH(c, bmk::median_pass(U, V, c->d_tmp, c->d_tmp + n, 1, fs, (int)p.sx_in, (int)p.sy_in, c->stream));
+        BM_LAUNCH(c, bmk::median_pass(c->d_tmp, c->d_tmp + n, c->d_flow_med, c->d_flow_med + n, 0, fs, (int)p.sx_in,
+                                      (int)p.sy_in, c->stream));
+        BM_LAUNCH(c, bmk::trilateral(U, V, c->d_flow_med, c->d_flow_med + n, d_prev_in, c->d_flow_out,
+                                     c->d_flow_out + n, (int)p.sx_in, (int)p.sy_in, c->tri_s, p.sEPE * p.sEPE,
+                                     p.sI * p.sI, p.sS * p.sS, c->stream));
+    } else {
+        BM_CUDA(cudaMemcpyAsync(c->d_flow_out, c->d_flow_in, 2 * n * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
+    }
+    return BM_OK;
+}
+
+bm_status set_pattern_impl(bm_ctx* c, const float* h_pattern)
+{
+    const uint32_t N = c->prm.N;
+    std::vector<int4> pat(N);
+    int rmax = 0;
+    for (uint32_t s = 0; s < N; s++) {
+        // int() truncation as in briefmatch_cuda.cu:110-113
+        int v[4];
+        for (int k = 0; k < 4; k++) {
+            v[k] = (int)h_pattern[4 * s + k];
+            rmax = std::max(rmax, std::abs(v[k]));
+        }
+        pat[s] = make_int4(v[0], v[1], v[2], v[3]);
+    }
+    BM_CUDA(cudaMemcpyAsync(c->d_pattern, pat.data(), N * sizeof(int4), cudaMemcpyHostToDevice, c->stream));
+    BM_CUDA(cudaStreamSynchronize(c->stream));
+    c->pattern_rmax = rmax;
+    return BM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* bm_last_error(void) { return g_last_error.c_str(); }
+
+const char* bm_version(void) { return "briefmatch_gb300 0.1 (sm_103a)"; }
+
+bm_status bm_create(const bm_params* prm, bm_ctx** out)
+{
+    if (!prm || !out) return fail(BM_ERR_INVALID, "bm_create: null argument");
+    *out = nullptr;
+    const bm_params& p = *prm;
+    // briefmatch.cpp:78-96
+    if (p.N > BM_PATCH_MAX / 4)
+        return fail(BM_ERR_LIMIT, "Feature length exceeds maximum value. Current size is %u and maximum is %d.", p.N,
+                    BM_PATCH_MAX / 4);
+    if (p.N < 1) return fail(BM_ERR_LIMIT, "Feature length must be at least 1.");
+    if (p.fsize > BM_MAX_MEDIAN)
+        return fail(BM_ERR_LIMIT, "Median filter size exceeds maximum value. Current size is %u and maximum is %d.",
+                    p.fsize, BM_MAX_MEDIAN);
+    if (std::ceil(p.sigma * 3) * 2 + 1 > BM_CONST_KERNEL_SIZE)
+        return fail(BM_ERR_LIMIT,
+                    "Maximum size of Gaussian down-sampling filter exceeded. Currently using sigma = %0.4f and "
+                    "maximum is %0.4f.",
+                    p.sigma, std::floor((BM_CONST_KERNEL_SIZE - 1.0f) / 2.0f) / 3.0f);
+    if (p.sx == 0 || p.sy == 0 || p.sx_in == 0 || p.sy_in == 0)
+        return fail(BM_ERR_INVALID, "bm_create: zero image size");
+    // the field is int16 (briefmatch.h:140-141)
+    if (p.sx > 32767 || p.sy > 32767)
+        return fail(BM_ERR_LIMIT, "Up-sampled size %ux%u exceeds the int16 flow range.", p.sx, p.sy);
+    if (p.rng != BM_RNG_XORWOW && p.rng != BM_RNG_PHILOX) return fail(BM_ERR_INVALID, "unknown rng %u", p.rng);
+
+    bm_ctx* c = new bm_ctx();
+    c->prm = p;
+    c->nsp = bmk::feature_stride(p.N);
+    c->npix = (size_t)p.sx * p.sy;
+    c->npix_in = (size_t)p.sx_in * p.sy_in;
+    float taps[BM_CONST_KERNEL_SIZE];
+    uint32_t P = 0;
+    bm_status st = bm_gauss_taps(p.sigma, taps, &P);
+    if (st != BM_OK) {
+        delete c;
+        return fail(st, "Gaussian taps could not be built for sigma %f", p.sigma);
+    }
+    c->prm.P = P;
+    c->dist = std::sqrt(std::ceil((float)p.sx * 0.5f / 3.0f));  // briefmatch.cpp:271
+    c->tri_s = (int)std::ceil(2.5 * (double)std::sqrt(p.sS * p.sS));  // briefmatch_cuda.cu:266
+
+#define BM_TRY(x)           \
+    do {                    \
+        st = (x);           \
+        if (st != BM_OK) {  \
+            release(c);     \
+            delete c;       \
+            return st;      \
+        }                   \
+    } while (0)
+    cudaError_t e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete c;
+        return fail(BM_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
+    }
+    c->stream = c->own_stream;
+    const size_t n = c->npix, ni = c->npix_in;
+    BM_TRY(dev_alloc(&c->d_frame_u8, ni));
+    BM_TRY(dev_alloc(&c->d_frame[0], ni));
+    BM_TRY(dev_alloc(&c->d_frame[1], ni));
+    BM_TRY(dev_alloc(&c->d_up, n));
+    BM_TRY(dev_alloc(&c->d_feat[0], n * c->nsp));
+    BM_TRY(dev_alloc(&c->d_feat[1], n * c->nsp));
+    BM_TRY(dev_alloc(&c->d_flow[0], n));
+    BM_TRY(dev_alloc(&c->d_flow[1], n));
+    BM_TRY(dev_alloc(&c->d_cost, n));
+    BM_TRY(dev_alloc(&c->d_flow_in, 2 * ni));
+    BM_TRY(dev_alloc(&c->d_flow_med, 2 * ni));
+    BM_TRY(dev_alloc(&c->d_flow_out, 2 * ni));
+    BM_TRY(dev_alloc(&c->d_tmp, 2 * ni));
+    BM_TRY(dev_alloc(&c->d_pattern, BM_PATCH_MAX / 4));
+    BM_TRY(dev_alloc(&c->d_taps, BM_CONST_KERNEL_SIZE));
+    BM_TRY(dev_alloc(&c->d_lx, (size_t)p.sx * 6));
+    BM_TRY(dev_alloc(&c->d_ix, (size_t)p.sx));
+    BM_TRY(dev_alloc(&c->d_ly, (size_t)p.sy * 6));
+    BM_TRY(dev_alloc(&c->d_iy, (size_t)p.sy));
+    BM_TRY(dev_alloc(&c->d_nnx, (size_t)p.sx_in));
+    BM_TRY(dev_alloc(&c->d_nny, (size_t)p.sy_in));
+#undef BM_TRY
+    auto cu = [&](cudaError_t err) -> bool {
+        if (err != cudaSuccess) {
+            fail(BM_ERR_CUDA, "bm_create: %s", cudaGetErrorString(err));
+            release(c);
+            delete c;
+            return false;
+        }
+        return true;
+    };
+    // zeroed descriptors and field: the first pair of a sequence starts from defined state
+    if (!cu(cudaMemsetAsync(c->d_feat[0], 0, n * c->nsp * sizeof(uint32_t), c->stream))) return BM_ERR_CUDA;
+    if (!cu(cudaMemsetAsync(c->d_feat[1], 0, n * c->nsp * sizeof(uint32_t), c->stream))) return BM_ERR_CUDA;
+    if (!cu(cudaMemsetAsync(c->d_flow[0], 0, n * sizeof(uint32_t), c->stream))) return BM_ERR_CUDA;
+    if (!cu(cudaMemsetAsync(c->d_flow[1], 0, n * sizeof(uint32_t), c->stream))) return BM_ERR_CUDA;
+    if (!cu(cudaMemsetAsync(c->d_cost, 0, n * sizeof(uint16_t), c->stream))) return BM_ERR_CUDA;
+    if (!cu(cudaMemsetAsync(c->d_flow_out, 0, 2 * ni * sizeof(float), c->stream))) return BM_ERR_CUDA;
+    if (!cu(cudaMemsetAsync(c->d_frame[0], 0, ni * sizeof(float), c->stream))) return BM_ERR_CUDA;
+    if (!cu(cudaMemsetAsync(c->d_frame[1], 0, ni * sizeof(float), c->stream))) return BM_ERR_CUDA;
+    if (!cu(cudaMemcpyAsync(c->d_taps, taps, P * sizeof(float), cudaMemcpyHostToDevice, c->stream))) return BM_ERR_CUDA;
+    if (!cu(bmk::lanczos_tables(c->d_lx, c->d_ix, (int)p.sx_in, (int)p.sx, c->stream))) return BM_ERR_CUDA;
+    if (!cu(bmk::lanczos_tables(c->d_ly, c->d_iy, (int)p.sy_in, (int)p.sy, c->stream))) return BM_ERR_CUDA;
+    if (!cu(bmk::nn_table(c->d_nnx, (int)p.sx, (int)p.sx_in, c->stream))) return BM_ERR_CUDA;
+    if (!cu(bmk::nn_table(c->d_nny, (int)p.sy, (int)p.sy_in, c->stream))) return BM_ERR_CUDA;
+    c->launches += 4;
+    std::vector<float> pattern(4 * (size_t)p.N);
+    bm_make_pattern(&c->prm, 0, pattern.data());
+    st = set_pattern_impl(c, pattern.data());
+    if (st != BM_OK) {
+        release(c);
+        delete c;
+        return st;
+    }
+    *out = c;
+    return BM_OK;
+}
+
+bm_status bm_destroy(bm_ctx* c)
+{
+    if (!c) return BM_OK;
+    cudaStreamSynchronize(c->stream);
+    release(c);
+    delete c;
+    return BM_OK;
+}
+
+bm_status bm_get_params(const bm_ctx* c, bm_params* out)
+{
+    if (!c || !out) return fail(BM_ERR_INVALID, "bm_get_params: null argument");
+    *out = c->prm;
+    return BM_OK;
+}
+
+bm_status bm_set_stream(bm_ctx* c, void* stream)
+{
+    if (check_ctx(c)) return BM_ERR_INVALID;
+    c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+    return BM_OK;
+}
+
+bm_status bm_synchronize(bm_ctx* c)
+{
+    if (check_ctx(c)) return BM_ERR_INVALID;
+    BM_CUDA(cudaStreamSynchronize(c->stream));
+    return BM_OK;
+}
+
+bm_status bm_set_pattern(bm_ctx* c, const float* h_pattern, uint32_t count)
+{
+    if (check_ctx(c)) return BM_ERR_INVALID;
+    if (!h_pattern) return fail(BM_ERR_INVALID, "bm_set_pattern: null pattern");
+    if (count != 4 * c->prm.N)
+        return fail(BM_ERR_INVALID, "bm_set_pattern: expected %u values (4*N), got %u", 4 * c->prm.N, count);
+    return set_pattern_impl(c, h_pattern);
+}
+
+uint32_t bm_feature_stride(const bm_ctx* c) { return c ? c->nsp : 0; }
+
+bm_status bm_read_buffer(bm_ctx* c, bm_buffer_id id, void* dst, size_t bytes, int dst_on_device)
+{
+    void* src = nullptr;
+    size_t cap = 0;
+    bm_status st = bm_buffer(c, id, &src, &cap);
+    if (st != BM_OK) return st;
+    if (!dst) return fail(BM_ERR_INVALID, "bm_read_buffer: null destination");
+    if (bytes > cap) return fail(BM_ERR_INVALID, "bm_read_buffer: %zu bytes requested, buffer holds %zu", bytes, cap);
+    BM_CUDA(cudaMemcpyAsync(dst, src, bytes, dst_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                            c->stream));
+    if (!dst_on_device) BM_CUDA(cudaStreamSynchronize(c->stream));
+    return BM_OK;
+}
+
+bm_status bm_write_buffer(bm_ctx* c, bm_buffer_id id, const void* src, size_t bytes, int src_on_device)
+{
+    void* dst = nullptr;
+    size_t cap = 0;
+    bm_status st = bm_buffer(c, id, &dst, &cap);
+    if (st != BM_OK) return st;
+    if (!src) return fail(BM_ERR_INVALID, "bm_write_buffer: null source");
+    if (bytes > cap) return fail(BM_ERR_INVALID, "bm_write_buffer: %zu bytes given, buffer holds %zu", bytes, cap);
+    BM_CUDA(cudaMemcpyAsync(dst, src, bytes, src_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                            c->stream));
+    if (!src_on_device) BM_CUDA(cudaStreamSynchronize(c->stream));
+    return BM_OK;
+}
+
+bm_status bm_buffer(bm_ctx* c, bm_buffer_id id, void** d_ptr, size_t* bytes)
+{
+    if (check_ctx(c)) return BM_ERR_INVALID;
+    if (!d_ptr) return fail(BM_ERR_INVALID, "bm_buffer: null output");
+    const size_t n = c->npix, ni = c->npix_in;
+    void* p = nullptr;
+    size_t b = 0;
+    switch (id) {
+    case BM_BUF_FEAT1: p = c->feat1_ptr(); b = n * c->nsp * 4; break;
+    case BM_BUF_FEAT2: p = c->feat2_ptr(); b = n * c->nsp * 4; break;
+    case BM_BUF_FLOW: p = c->d_flow[c->flow_cur]; b = n * 4; break;
+    case BM_BUF_COST: p = c->d_cost; b = n * 2; break;
+    case BM_BUF_UP: p = c->d_up; b = n * 4; break;
+    case BM_BUF_FLOW_IN: p = c->d_flow_in; b = 2 * ni * 4; break;
+    case BM_BUF_FLOW_MED: p = c->d_flow_med; b = 2 * ni * 4; break;
+    case BM_BUF_FLOW_OUT: p = c->d_flow_out; b = 2 * ni * 4; break;
+    case BM_BUF_FRAME: p = c->d_frame[c->cur_frame]; b = ni * 4; break;
+    case BM_BUF_FRAME_PREV: p = c->d_frame[c->cur_frame ^ 1]; b = ni * 4; break;
+    default: return fail(BM_ERR_INVALID, "bm_buffer: unknown id %d", (int)id);
+    }
+    *d_ptr = p;
+    if (bytes) *bytes = b;
+    return BM_OK;
+}
+
+bm_status bm_upsample(bm_ctx* c, const float* d_in, float* d_out)
+{
+    if (check_ctx(c)) return BM_ERR_INVALID;
+    if (!d_in || !d_out) return fail(BM_ERR_INVALID, "bm_upsample: null buffer");
+    const bm_params& p = c->prm;
+    BM_LAUNCH(c, bmk::upsample_f32(d_in, d_out, (int)p.sx_in, (int)p.sy_in, (int)p.sx, (int)p.sy, c->d_lx, c->d_ix,
+                                   c->d_ly, c->d_iy, c->stream));
+    return BM_OK;
+}
+
+bm_status bm_upsample_u8(bm_ctx* c, const uint8_t* d_in, float* d_out)
+{
+    if (check_ctx(c)) return BM_ERR_INVALID;
+    if (!d_in || !d_out) return fail(BM_ERR_INVALID, "bm_upsample_u8: null buffer");
+    const bm_params& p = c->prm;
+    BM_LAUNCH(c, bmk::upsample_u8(d_in, d_out, (int)p.sx_in, (int)p.sy_in, (int)p.sx, (int)p.sy, c->d_lx, c->d_ix,
+                                  c->d_ly, c->d_iy, c->stream));
+    return BM_OK;
+}
+
+bm_status bm_features(bm_ctx* c, const float* d_up, int slot)
+{
+    if (check_ctx(c)) return BM_ERR_INVALID;
+    if (!d_up) return fail(BM_ERR_INVALID, "bm_features: null image");
+    if (slot != 0 && slot != 1) return fail(BM_ERR_INVALID, "bm_features: slot must be 0 or 1");
+    return features_into(c, d_up, slot == 0 ? c->feat1_ptr() : c->feat2_ptr());
+}
+
+bm_status bm_initialize(bm_ctx* c, int first)
+{
+    if (check_ctx(c)) return BM_ERR_INVALID;
+    const bm_params& p = c->prm;
+    BM_LAUNCH(c, bmk::initialize(c->feat1_ptr(), c->feat2_ptr(), c->d_flow[c->flow_cur], c->d_flow[c->flow_cur ^ 1],
+                                 c->d_cost, (int)p.sx, (int)p.sy, (int)c->nsp, first ? 1 : 0, c->stream));
+    c->flow_cur ^= 1;
+    return BM_OK;
+}
+
+bm_status bm_propagate(bm_ctx* c, int pd)
+{
+    if (check_ctx(c)) return BM_ERR_INVALID;
+    return propagate_pass(c, pd, false);
+}
+
+bm_status bm_random_search(bm_ctx* c)
+{
+    if (check_ctx(c)) return BM_ERR_INVALID;
+    const bm_params& p = c->prm;
+    bmk::RsArgs rs = rs_args(c, true);
+    BM_LAUNCH(c, bmk::random_search(c->feat1_ptr(), c->feat2_ptr(), c->d_flow[c->flow_cur], c->d_cost, (int)p.sx,
+                                    (int)p.sy, (int)c->nsp, rs, c->stream));
+    c->rs_calls++;
+    return BM_OK;
+}
+
+bm_status bm_match(bm_ctx* c, const float* d_im1, const float* d_im2)
+{
+    (void)d_im1;
+    if (check_ctx(c)) return BM_ERR_INVALID;
+    if (!d_im2) return fail(BM_ERR_INVALID, "bm_match: null frame");
+    return match_impl(c, d_im2);
+}
+
+bm_status bm_downsample(bm_ctx* c)
+{
+    if (check_ctx(c)) return BM_ERR_INVALID;
+    return downsample_impl(c);
+}
+
+bm_status bm_process(bm_ctx* c, const float* d_prev_in)
+{
+    if (check_ctx(c)) return BM_ERR_INVALID;
+    return process_impl(c, d_prev_in);
+}
+
+bm_status bm_swap(bm_ctx* c)
+{
+    if (check_ctx(c)) return BM_ERR_INVALID;
+    c->feat1 ^= 1;
+    return BM_OK;
+}
+
+bm_status bm_convert(bm_ctx* c, float* h_u, float* h_v)
+{
+    if (check_ctx(c)) return BM_ERR_INVALID;
+    if (!h_u || !h_v) return fail(BM_ERR_INVALID, "bm_convert: null output");
+    const size_t b = c->npix_in * sizeof(float);
+    BM_CUDA(cudaMemcpyAsync(h_u, c->d_flow_out, b, cudaMemcpyDeviceToHost, c->stream));
+    BM_CUDA(cudaMemcpyAsync(h_v, c->d_flow_out + c->npix_in, b, cudaMemcpyDeviceToHost, c->stream));
+    BM_CUDA(cudaStreamSynchronize(c->stream));
+    return BM_OK;
+}
+
+bm_status bm_export_field(bm_ctx* c, int16_t* d_nx, int16_t* d_ny, float* d_dist)
+{
+    if (check_ctx(c)) return BM_ERR_INVALID;
+    BM_LAUNCH(c, bmk::export_field(c->d_flow[c->flow_cur], c->d_cost, d_nx, d_ny, d_dist, c->npix, (int)c->prm.N,
+                                   c->stream));
+    return BM_OK;
+}
+
+bm_status bm_import_field(bm_ctx* c, const int16_t* d_nx, const int16_t* d_ny, const uint16_t* d_cost)
+{
+    if (check_ctx(c)) return BM_ERR_INVALID;
+    if (!d_nx || !d_ny) return fail(BM_ERR_INVALID, "bm_import_field: null field");
+    BM_LAUNCH(c, bmk::import_field(d_nx, d_ny, d_cost, c->d_flow[c->flow_cur], c->d_cost, c->npix, c->stream));
+    return BM_OK;
+}
+
+bm_status bm_normals(bm_ctx* c, uint64_t call, float* d_out)
+{
+    if (check_ctx(c)) return BM_ERR_INVALID;
+    if (!d_out) return fail(BM_ERR_INVALID, "bm_normals: null output");
+    bmk::RsArgs rs = rs_args(c, true);
+    rs.call = call;
+    BM_LAUNCH(c, bmk::normals(reinterpret_cast<float2*>(d_out), (int)c->prm.sx, (int)c->prm.sy, rs, c->stream));
+    return BM_OK;
+}
+
+bm_status bm_nn_indices(bm_ctx* c, uint32_t* h_x, uint32_t* h_y)
+{
+    if (check_ctx(c)) return BM_ERR_INVALID;
+    if (!h_x || !h_y) return fail(BM_ERR_INVALID, "bm_nn_indices: null output");
+    BM_CUDA(cudaMemcpyAsync(h_x, c->d_nnx, c->prm.sx_in * sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
+    BM_CUDA(cudaMemcpyAsync(h_y, c->d_nny, c->prm.sy_in * sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
+    BM_CUDA(cudaStreamSynchronize(c->stream));
+    return BM_OK;
+}
+
+bm_status bm_rng_position(bm_ctx* c, uint64_t* calls)
+{
+    if (check_ctx(c) || !calls) return fail(BM_ERR_INVALID, "bm_rng_position: null argument");
+    *calls = c->rs_calls;
+    return BM_OK;
+}
+
+bm_status bm_set_rng_position(bm_ctx* c, uint64_t calls)
+{
+    if (check_ctx(c)) return BM_ERR_INVALID;
+    c->rs_calls = calls;
+    return BM_OK;
+}
+
+bm_status bm_reset_sequence(bm_ctx* c)
+{
+    if (check_ctx(c)) return BM_ERR_INVALID;
+    c->primed = false;
+    c->first_match = true;
+    return BM_OK;
+}
+
+uint64_t bm_launch_count(const bm_ctx* c) { return c ? c->launches : 0; }
+
+bm_status bm_frame(bm_ctx* c, const uint8_t* frame, int frame_on_device, float* u, float* v, int out_on_device)
+{
+    if (check_ctx(c)) return BM_ERR_INVALID;
+    if (!frame) return fail(BM_ERR_INVALID, "bm_frame: null frame");
+    const bm_params& p = c->prm;
+    const size_t ni = c->npix_in;
+    const uint8_t* d_u8 = frame;
+    if (!frame_on_device) {
+        // of_pipeline.cpp:297 (8-bit here: a quarter of the reference's float copy)
+        BM_CUDA(cudaMemcpyAsync(c->d_frame_u8, frame, ni, cudaMemcpyHostToDevice, c->stream));
+        d_u8 = c->d_frame_u8;
+    }
+    float* cur = c->d_frame[c->cur_frame];
+    BM_LAUNCH(c, bmk::u8_to_f32(d_u8, cur, ni, c->stream));
+    // of_pipeline.cpp:301-310
+    const float* up = cur;
+    if (p.sx != p.sx_in || p.sy != p.sy_in) {
+        BM_LAUNCH(c, bmk::upsample_u8(d_u8, c->d_up, (int)p.sx_in, (int)p.sy_in, (int)p.sx, (int)p.sy, c->d_lx, c->d_ix,
+                                      c->d_ly, c->d_iy, c->stream));
+        up = c->d_up;
+    }
+    bm_status st;
+    if (!c->primed) {
+        st = features_into(c, up, c->feat2_ptr());
+        if (st != BM_OK) return st;
+        BM_CUDA(cudaMemsetAsync(c->d_flow_out, 0, 2 * ni * sizeof(float), c->stream));
+        c->primed = true;
+    } else {
+        st = match_impl(c, up);                                   // of_pipeline.cpp:314
+        if (st == BM_OK) st = downsample_impl(c);                 // :319
+        if (st == BM_OK) st = process_impl(c, c->d_frame[c->cur_frame ^ 1]);  // :324
+        if (st != BM_OK) return st;
+    }
+    // of_pipeline.cpp:331-333
+    c->cur_frame ^= 1;
+    c->feat1 ^= 1;
+    if (u || v) {
+        const cudaMemcpyKind kind = out_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+        if (u) BM_CUDA(cudaMemcpyAsync(u, c->d_flow_out, ni * sizeof(float), kind, c->stream));
+        if (v) BM_CUDA(cudaMemcpyAsync(v, c->d_flow_out + ni, ni * sizeof(float), kind, c->stream));
+        if (!out_on_device) BM_CUDA(cudaStreamSynchronize(c->stream));
+    }
+    return BM_OK;
+}
+
+}  // extern "C"

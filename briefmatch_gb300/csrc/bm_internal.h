@@ -1,0 +1,78 @@
+// bm_internal.h -- engine-private declarations shared by the kernel and API units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stddef.h>
+
+#include "briefmatch_gb300.h"
+
+namespace bmk {
+
+// Random-search stream position for one launch (briefmatch_cuda.cu:237-241).
+struct RsArgs {
+    int enabled;                 // fuse a random-search candidate into the launch
+    int mode;                    // BM_RNG_XORWOW or BM_RNG_PHILOX
+    unsigned long long seed;     // Philox key
+    unsigned long long call;     // index of this random-search call in the stream
+    float dist;                  // search radius, briefmatch.cpp:271
+};
+
+// Flow words: low 16 bits nx, high 16 bits ny, both int16.
+__host__ __device__ inline uint32_t pack_flow(int nx, int ny)
+{
+    return (uint32_t)(uint16_t)(int16_t)nx | ((uint32_t)(uint16_t)(int16_t)ny << 16);
+}
+
+// Words per descriptor in the engine layout: ceil(N/32) rounded up to 1, 2, 4, 8 or 16.
+inline uint32_t feature_stride(uint32_t N)
+{
+    uint32_t ns = (N + 31) / 32;
+    uint32_t s = 1;
+    while (s < ns) s <<= 1;
+    return s;
+}
+
+cudaError_t lanczos_tables(float* w, int* idx, int n_in, int n_out, cudaStream_t st);
+cudaError_t upsample_f32(const float* in, float* out, int sxi, int syi, int sxo, int syo,
+                         const float* lx, const int* ix, const float* ly, const int* iy, cudaStream_t st);
+cudaError_t upsample_u8(const uint8_t* in, float* out, int sxi, int syi, int sxo, int syo,
+                        const float* lx, const int* ix, const float* ly, const int* iy, cudaStream_t st);
+cudaError_t u8_to_f32(const uint8_t* in, float* out, size_t n, cudaStream_t st);
+
+cudaError_t features(const float* up, uint32_t* F, int sx, int sy, int N, int nsp,
+                     const int4* pat, int rmax, cudaStream_t st);
+
+cudaError_t initialize(const uint32_t* F1, const uint32_t* F2, const uint32_t* flow_prev,
+                       uint32_t* flow_out, uint16_t* cost, int sx, int sy, int nsp, int first,
+                       cudaStream_t st);
+
+cudaError_t jump_level(const uint32_t* F1, const uint32_t* F2, const uint32_t* flow_in,
+                       uint32_t* flow_out, uint16_t* cost, int sx, int sy, int nsp,
+                       int p, int pd, int doubleProp, const RsArgs& rs, cudaStream_t st);
+
+cudaError_t random_search(const uint32_t* F1, const uint32_t* F2, uint32_t* flow, uint16_t* cost,
+                          int sx, int sy, int nsp, const RsArgs& rs, cudaStream_t st);
+
+cudaError_t normals(float2* out, int sx, int sy, const RsArgs& rs, cudaStream_t st);
+
+cudaError_t nn_table(unsigned int* idx, int n_up, int n_in, cudaStream_t st);
+cudaError_t downsample(const uint32_t* flow, float* U, float* V, int sx, int sy, int sx_in, int sy_in,
+                       const float* taps, int P, float mx, float my, const unsigned int* nnx,
+                       const unsigned int* nny, cudaStream_t st);
+
+cudaError_t flow_to_planes(const uint32_t* flow, float* U, float* V, size_t n, cudaStream_t st);
+
+cudaError_t median_pass(const float* inU, const float* inV, float* outU, float* outV,
+                        int dir, int fsize, int sx, int sy, cudaStream_t st);
+
+cudaError_t trilateral(const float* U, const float* V, const float* Um, const float* Vm,
+                       const float* I, float* Uo, float* Vo, int sx, int sy, int s,
+                       float sigmaEPE2, float sigmaI2, float sigmaS2, cudaStream_t st);
+
+cudaError_t export_field(const uint32_t* flow, const uint16_t* cost, int16_t* nx, int16_t* ny,
+                         float* dist, size_t n, int N, cudaStream_t st);
+cudaError_t import_field(const int16_t* nx, const int16_t* ny, const uint16_t* cost_in,
+                         uint32_t* flow, uint16_t* cost, size_t n, cudaStream_t st);
+
+}  // namespace bmk

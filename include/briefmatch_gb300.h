@@ -1,0 +1,219 @@
+/*
+ * briefmatch_gb300.h -- C ABI of the GB300 BriefMatch flow engine.
+ *
+ * The engine replaces the reference's kernel layer (kernels/briefmatch_cuda.h:64-93,
+ * kernels/util_cuda.h:114-129) and the device-side sequencing of BriefMatch
+ * (briefmatch.cpp:72-352) and OFPipeline::processFrame (of_pipeline.cpp:241-333).
+ * Each entry point names the reference function it stands in for.
+ *
+ * Conventions
+ *   - Every call returns a bm_status; nothing throws across this boundary.  The
+ *     text of the last error on the calling thread is bm_last_error().
+ *   - Sizes are size_t / uint32_t; there is no int-sized allocation limit.
+ *   - Arguments named d_* are device pointers, h_* host pointers.
+ *   - Work is queued on the context's stream (bm_set_stream); calls that return
+ *     host data synchronise that stream before returning.
+ *   - A context owns its device buffers, its BRIEF sampling pattern and its
+ *     down-sampling taps, so several contexts can coexist in one process (the
+ *     reference keeps these in process-wide __constant__ memory).
+ */
+#ifndef BRIEFMATCH_GB300_H
+#define BRIEFMATCH_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BM_PATCH_MAX 2048          /* briefmatch_cuda.h:62: 4 floats per sample, N <= 512 */
+#define BM_MAX_MEDIAN 47           /* util_cuda.h:56 */
+#define BM_CONST_KERNEL_SIZE 100   /* util_cuda.h:58 */
+
+typedef enum bm_status {
+    BM_OK = 0,
+    BM_ERR_INVALID = 1,  /* null pointer, zero size, unknown id */
+    BM_ERR_LIMIT = 2,    /* a parameter beyond a limit (BriefMatchException, briefmatch.cpp:78-96) */
+    BM_ERR_CUDA = 3,     /* CUDA runtime error (CudaException, util_cuda.h:85-112) */
+    BM_ERR_STATE = 4,    /* call out of order (BriefMatchException, briefmatch.cpp:251) */
+    BM_ERR_NOMEM = 5,    /* device or host allocation failed */
+    BM_ERR_TIMEOUT = 6,  /* a bounded device-side wait gave up */
+    BM_ERR_IO = 7        /* file could not be read or written */
+} bm_status;
+
+/* Random stream used by the random search (briefmatch_cuda.cu:237-245). */
+enum {
+    BM_RNG_XORWOW = 0,   /* the reference stream: curand_init(pixel, 0, 0) + curand_normal */
+    BM_RNG_PHILOX = 1    /* counter-based: Philox4x32-10 (subsequence = pixel) seeded by bm_params.seed */
+};
+
+/* BMParams, briefmatch.h:65-89 (same fields, same defaults), plus the RNG choice. */
+typedef struct bm_params {
+    uint32_t sx, sy;          /* up-sampled (matching) resolution */
+    uint32_t sx_in, sy_in;    /* input resolution */
+    uint32_t N;               /* descriptor length in bits, 2..512 */
+    uint32_t iterations;      /* propagation + random-search rounds */
+    uint32_t jfMax;           /* largest jump-flood step */
+    uint32_t P;               /* Gaussian down-sampling taps (derived from sigma at create) */
+    uint32_t fsize;           /* median window */
+    float patchArea;          /* BRIEF sampling radius, up-sampled pixels */
+    float sigma;              /* Gaussian down-sampling sigma, up-sampled pixels */
+    float sEPE, sI, sS;       /* trilateral filter sigmas (flow, intensity, spatial) */
+    float maxmot;             /* colour-coding clamp */
+    int32_t doubleProp;       /* propagate in both directions per level */
+    int32_t filter;           /* run median + trilateral refinement */
+    int32_t tInit;            /* temporal initialisation from the previous pair */
+    uint32_t rng;             /* BM_RNG_XORWOW or BM_RNG_PHILOX */
+    uint64_t seed;            /* seed of the Philox stream */
+} bm_params;
+
+typedef struct bm_ctx bm_ctx;
+
+/* Device buffers a context exposes (bm_buffer). */
+typedef enum bm_buffer_id {
+    BM_BUF_FEAT1 = 0,      /* uint32 descriptors of frame 1 (previous), [sx*sy][stride] */
+    BM_BUF_FEAT2 = 1,      /* uint32 descriptors of frame 2 (current) */
+    BM_BUF_FLOW = 2,       /* uint32 packed field: low 16 bits nx, high 16 bits ny (int16 each) */
+    BM_BUF_COST = 3,       /* uint16 Hamming distance of the current field */
+    BM_BUF_UP = 4,         /* float up-sampled current frame, sx*sy */
+    BM_BUF_FLOW_IN = 5,    /* float2 planes U then V: down-sampled field, sx_in*sy_in each */
+    BM_BUF_FLOW_MED = 6,   /* float planes U then V: median-filtered field */
+    BM_BUF_FLOW_OUT = 7,   /* float planes U then V: refined output field */
+    BM_BUF_FRAME = 8,      /* float current input frame, sx_in*sy_in */
+    BM_BUF_FRAME_PREV = 9  /* float previous input frame, sx_in*sy_in */
+} bm_buffer_id;
+
+/* ---- parameters (host only) ------------------------------------------------ */
+
+/* BMParams::BMParams, briefmatch.h:67-84. */
+bm_status bm_params_default(bm_params* p);
+
+/* Derivation of OFPipeline::setParams, of_pipeline.cpp:178-190: up-sampled size,
+ * patch radius, down-sampling sigma, median size and spatial sigma from the input
+ * size and the percentages given on the command line (ux/uy <= 0.1 select the
+ * defaults 2.740/3.052 as at :178-179). */
+bm_status bm_params_derive(bm_params* p, uint32_t width, uint32_t height, float ux, float uy,
+                           float patchRad, float sigmaRad, float fsizeRad, float sSRad);
+
+/* BRIEF sampling pattern, briefmatch.cpp:124-148: 4N values of sign(g)*g^2 with
+ * g ~ N(0, 0.2), clamped to [-1,1] and scaled by patchArea.  The reference seeds
+ * Boost's mt19937 from time(NULL); here the seed is explicit (std::mt19937_64). */
+bm_status bm_make_pattern(const bm_params* p, uint64_t seed, float* h_pattern /* 4*N */);
+
+/* Gaussian taps, briefmatch.cpp:153-172.  *P receives the tap count. */
+bm_status bm_gauss_taps(float sigma, float* h_taps /* BM_CONST_KERNEL_SIZE */, uint32_t* P);
+
+/* ---- context ------------------------------------------------------------------ */
+
+/* BriefMatch::setup, briefmatch.cpp:72-214: checks limits, allocates every device
+ * buffer, builds the taps and a default pattern (seed 0). */
+bm_status bm_create(const bm_params* p, bm_ctx** out);
+
+/* BriefMatch::clean, briefmatch.cpp:217-238. */
+bm_status bm_destroy(bm_ctx* ctx);
+
+/* BriefMatch::getParams, briefmatch.h:118 (P is the derived tap count). */
+bm_status bm_get_params(const bm_ctx* ctx, bm_params* out);
+
+/* Queue subsequent work on this cudaStream_t (NULL = the context's own stream). */
+bm_status bm_set_stream(bm_ctx* ctx, void* stream);
+bm_status bm_synchronize(bm_ctx* ctx);
+
+/* CUDA_copyPatchToConst, briefmatch_cuda.cu:376-379: install 4*N pattern values. */
+bm_status bm_set_pattern(bm_ctx* ctx, const float* h_pattern, uint32_t count);
+
+/* Pointer and byte size of one of the context's device buffers. */
+bm_status bm_buffer(bm_ctx* ctx, bm_buffer_id id, void** d_ptr, size_t* bytes);
+
+/* Copy bytes between a context buffer and caller memory (host or device memory
+ * per the *_on_device flag).  Host copies complete before the call returns. */
+bm_status bm_read_buffer(bm_ctx* ctx, bm_buffer_id id, void* dst, size_t bytes, int dst_on_device);
+bm_status bm_write_buffer(bm_ctx* ctx, bm_buffer_id id, const void* src, size_t bytes, int src_on_device);
+
+/* Words per descriptor in the context's layout (ceil(N/32) rounded up to 1,2,4,8,16). */
+uint32_t bm_feature_stride(const bm_ctx* ctx);
+
+/* ---- stages (device pointers; mirror the reference kernel layer) --------------- */
+
+/* CUDA_resizeLanczos, util_cuda.cu:250-257: Lanczos-3 from sx_in x sy_in to sx x sy. */
+bm_status bm_upsample(bm_ctx* ctx, const float* d_in, float* d_out);
+/* The same from 8-bit input (the frame read of of_pipeline.cpp:279-285 fused in). */
+bm_status bm_upsample_u8(bm_ctx* ctx, const uint8_t* d_in, float* d_out);
+
+/* CUDA_binaryFeatures, briefmatch_cuda.cu:311-319: descriptors of the up-sampled
+ * image d_up into FEAT1 (slot 0) or FEAT2 (slot 1). */
+bm_status bm_features(bm_ctx* ctx, const float* d_up, int slot);
+
+/* CUDA_initialize, briefmatch_cuda.cu:321-332. */
+bm_status bm_initialize(bm_ctx* ctx, int first);
+
+/* CUDA_propagate, briefmatch_cuda.cu:334-347: one jump-flood pass, direction pd. */
+bm_status bm_propagate(bm_ctx* ctx, int pd);
+
+/* CUDA_randomSearch, briefmatch_cuda.cu:349-360: one random candidate per pixel,
+ * drawn from the next position of the context's random stream. */
+bm_status bm_random_search(bm_ctx* ctx);
+
+/* BriefMatch::match, briefmatch.cpp:248-293: descriptors of d_im2 into FEAT2, then
+ * initialise and iterate.  d_im1 is accepted for signature parity and unused, as in
+ * the reference (the kernels only read descriptors). */
+bm_status bm_match(bm_ctx* ctx, const float* d_im1, const float* d_im2);
+
+/* BriefMatch::downsample, briefmatch.cpp:296-324. */
+bm_status bm_downsample(bm_ctx* ctx);
+
+/* BriefMatch::process, briefmatch.cpp:327-352: median + trilateral filter guided by
+ * d_prev_in, the previous input-resolution frame (float, 0..255). */
+bm_status bm_process(bm_ctx* ctx, const float* d_prev_in);
+
+/* BriefMatch::swap, briefmatch.cpp:240-245. */
+bm_status bm_swap(bm_ctx* ctx);
+
+/* BriefMatch::convert, briefmatch.cpp:355-370: copy the output field to the host. */
+bm_status bm_convert(bm_ctx* ctx, float* h_u, float* h_v);
+
+/* The field in the reference's layout (sint NX, NY and float D = H/N,
+ * briefmatch.h:139-141), written to device arrays of sx*sy elements. */
+bm_status bm_export_field(bm_ctx* ctx, int16_t* d_nx, int16_t* d_ny, float* d_dist);
+
+/* Load a field in the reference's layout into the context (recomputes nothing). */
+bm_status bm_import_field(bm_ctx* ctx, const int16_t* d_nx, const int16_t* d_ny, const uint16_t* d_cost);
+
+/* The N(0,1) pairs random-search call number `call` uses, as float2 per pixel. */
+bm_status bm_normals(bm_ctx* ctx, uint64_t call, float* d_out /* 2*sx*sy */);
+
+/* The source pixel resizeNN picks for every input column (h_x, sx_in values) and row
+ * (h_y, sy_in values), util_cuda.cu:165-166.  The reference computes the index with
+ * the device's fast division; so does the engine, and these tables expose it. */
+bm_status bm_nn_indices(bm_ctx* ctx, uint32_t* h_x, uint32_t* h_y);
+
+/* Position of the random stream: number of random-search calls made so far. */
+bm_status bm_rng_position(bm_ctx* ctx, uint64_t* calls);
+bm_status bm_set_rng_position(bm_ctx* ctx, uint64_t calls);
+
+/* ---- one frame (OFPipeline::processFrame, of_pipeline.cpp:241-333) --------------- */
+
+/* Feed the next 8-bit frame (sx_in*sy_in bytes, row-major).  frame_on_device says
+ * whether `frame` is a device pointer.  The first frame only primes the context
+ * (descriptors of that frame) and yields a zero field; every later frame runs
+ * up-sampling, matching against the previous frame, down-sampling and refinement
+ * and yields the flow from the previous frame to this one on the previous frame's
+ * grid.  u and v (sx_in*sy_in floats each, device or host per out_on_device) may be
+ * NULL to leave the result in BM_BUF_FLOW_OUT. */
+bm_status bm_frame(bm_ctx* ctx, const uint8_t* frame, int frame_on_device,
+                   float* u, float* v, int out_on_device);
+
+/* Forget the previous frame: the next bm_frame primes again. */
+bm_status bm_reset_sequence(bm_ctx* ctx);
+
+/* Count of kernels this context has launched (for launch accounting). */
+uint64_t bm_launch_count(const bm_ctx* ctx);
+
+const char* bm_last_error(void);
+const char* bm_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

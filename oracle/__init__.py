@@ -1,0 +1,252 @@
+"""The oracle: CPU restatement of the BriefMatch flow path (TEST INFRASTRUCTURE).
+
+Only the tests, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg may use
+this package, and only as the checker or the timed CPU baseline, never as the
+engine.  It wraps oracle/_build/libbmoracle.so (bm_oracle.c) with numpy arrays in
+the reference's layouts: float images, uint32 descriptors [sx*sy][ceil(N/32)],
+int16 NX/NY, uint16 Hamming costs.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_LIB = os.path.join(_HERE, "_build", "libbmoracle.so")
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(ORACLE_LIB):
+            raise ImportError("oracle library missing at %s; run __graft_entry__.build()" % ORACLE_LIB)
+        L = ctypes.CDLL(ORACLE_LIB)
+        vp, i, f, u64, sz = ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.c_uint64, ctypes.c_size_t
+        sig = {
+            "bmo_num_threads": (i, []),
+            "bmo_set_threads": (None, [i]),
+            "bmo_upsample": (None, [vp, i, i, vp, i, i]),
+            "bmo_u8_to_float": (None, [vp, sz, vp]),
+            "bmo_features": (None, [vp, i, i, vp, i, vp]),
+            "bmo_initialize": (None, [vp, vp, i, i, i, i, vp, vp, vp]),
+            "bmo_jump_level": (None, [vp, vp, i, i, i, i, i, i, vp, vp, vp, vp, vp]),
+            "bmo_propagate": (None, [vp, vp, i, i, i, i, i, i, vp, vp, vp]),
+            "bmo_random_search": (None, [vp, vp, i, i, i, f, vp, vp, vp, vp]),
+            "bmo_match": (None, [vp, vp, i, i, i, i, i, i, i, f, vp, vp, vp, vp]),
+            "bmo_search_dist": (f, [i]),
+            "bmo_gauss_taps": (i, [f, vp, i]),
+            "bmo_downsample": (None, [vp, vp, i, i, i, i, vp, i, vp, vp, vp, vp]),
+            "bmo_median1d": (None, [vp, vp, i, i, i, i]),
+            "bmo_trilateral": (None, [vp, vp, vp, vp, vp, f, f, f, i, i, vp, vp]),
+            "bmo_refine": (None, [vp, vp, vp, i, i, i, f, f, f, vp, vp, vp, vp]),
+            "bmo_epe": (ctypes.c_double, [vp, vp, vp, vp, sz]),
+            "bmo_normals": (None, [u64, sz, vp]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _c(a, dtype):
+    a = np.ascontiguousarray(a, dtype=dtype)
+    return a
+
+
+def _p(a):
+    return a.ctypes.data
+
+
+def num_threads():
+    return lib().bmo_num_threads()
+
+
+def set_threads(n):
+    lib().bmo_set_threads(int(n))
+
+
+def upsample(img, sxo, syo):
+    img = _c(img, np.float32)
+    syi, sxi = img.shape
+    out = np.empty((syo, sxo), np.float32)
+    lib().bmo_upsample(_p(img), sxi, syi, _p(out), sxo, syo)
+    return out
+
+
+def features(I, pattern, N):
+    I = _c(I, np.float32)
+    pattern = _c(pattern, np.float32)
+    sy, sx = I.shape
+    ns = (N + 31) // 32
+    F = np.empty((sy * sx, ns), np.uint32)
+    lib().bmo_features(_p(I), sx, sy, _p(pattern), N, _p(F))
+    return F
+
+
+def initialize(F1, F2, sx, sy, N, first, NX=None, NY=None):
+    n = sx * sy
+    NX = np.zeros(n, np.int16) if NX is None else _c(NX, np.int16).copy()
+    NY = np.zeros(n, np.int16) if NY is None else _c(NY, np.int16).copy()
+    H = np.zeros(n, np.uint16)
+    lib().bmo_initialize(_p(_c(F1, np.uint32)), _p(_c(F2, np.uint32)), sx, sy, N, int(bool(first)), _p(NX), _p(NY), _p(H))
+    return NX, NY, H
+
+
+def jump_level(F1, F2, sx, sy, N, p, pd, double_prop, NX, NY, H):
+    NXs = _c(NX, np.int16).copy()
+    NYs = _c(NY, np.int16).copy()
+    NXo, NYo, Ho = NXs.copy(), NYs.copy(), _c(H, np.uint16).copy()
+    lib().bmo_jump_level(_p(_c(F1, np.uint32)), _p(_c(F2, np.uint32)), sx, sy, N, p, pd, int(bool(double_prop)),
+                         _p(NXs), _p(NYs), _p(NXo), _p(NYo), _p(Ho))
+    return NXo, NYo, Ho
+
+
+def propagate(F1, F2, sx, sy, N, pd, jf_max, double_prop, NX, NY, H):
+    NX, NY, H = _c(NX, np.int16).copy(), _c(NY, np.int16).copy(), _c(H, np.uint16).copy()
+    lib().bmo_propagate(_p(_c(F1, np.uint32)), _p(_c(F2, np.uint32)), sx, sy, N, pd, jf_max, int(bool(double_prop)),
+                        _p(NX), _p(NY), _p(H))
+    return NX, NY, H
+
+
+def random_search(F1, F2, sx, sy, N, dist, normals, NX, NY, H):
+    NX, NY, H = _c(NX, np.int16).copy(), _c(NY, np.int16).copy(), _c(H, np.uint16).copy()
+    nrm = _c(normals, np.float32)
+    lib().bmo_random_search(_p(_c(F1, np.uint32)), _p(_c(F2, np.uint32)), sx, sy, N, dist, _p(nrm), _p(NX), _p(NY), _p(H))
+    return NX, NY, H
+
+
+def match(F1, F2, sx, sy, N, iterations, jf_max, double_prop, first, dist, normals, NX=None, NY=None):
+    n = sx * sy
+    NX = np.zeros(n, np.int16) if NX is None else _c(NX, np.int16).copy()
+    NY = np.zeros(n, np.int16) if NY is None else _c(NY, np.int16).copy()
+    H = np.zeros(n, np.uint16)
+    nrm = _c(normals, np.float32)
+    assert nrm.size >= iterations * n * 2
+    lib().bmo_match(_p(_c(F1, np.uint32)), _p(_c(F2, np.uint32)), sx, sy, N, iterations, jf_max, int(bool(double_prop)),
+                    int(bool(first)), dist, _p(nrm), _p(NX), _p(NY), _p(H))
+    return NX, NY, H
+
+
+def search_dist(sx):
+    return lib().bmo_search_dist(sx)
+
+
+def gauss_taps(sigma):
+    out = np.zeros(100, np.float32)
+    P = lib().bmo_gauss_taps(sigma, _p(out), 100)
+    if P < 0:
+        raise ValueError("sigma too large")
+    return out[:P].copy()
+
+
+def downsample(NX, NY, sx, sy, sx_in, sy_in, taps, nn=None):
+    """nn = (xs, ys): the device's resizeNN index tables (bm_nn_indices); None
+    computes them with IEEE division."""
+    taps = _c(taps, np.float32)
+    U = np.zeros((sy_in, sx_in), np.float32)
+    V = np.zeros((sy_in, sx_in), np.float32)
+    if nn is None:
+        px = py = None
+    else:
+        xs, ys = _c(nn[0], np.uint32), _c(nn[1], np.uint32)
+        assert xs.size == sx_in and ys.size == sy_in
+        px, py = _p(xs), _p(ys)
+    lib().bmo_downsample(_p(_c(NX, np.int16)), _p(_c(NY, np.int16)), sx, sy, sx_in, sy_in, _p(taps), taps.size,
+                         px, py, _p(U), _p(V))
+    return U, V
+
+
+def median1d(a, direction, fsize):
+    a = _c(a, np.float32)
+    sy, sx = a.shape
+    out = np.empty_like(a)
+    lib().bmo_median1d(_p(a), _p(out), direction, fsize, sx, sy)
+    return out
+
+
+def trilateral(U, V, Um, Vm, I, sEPE2, sI2, sS2):
+    U, V, Um, Vm, I = (_c(a, np.float32) for a in (U, V, Um, Vm, I))
+    sy, sx = U.shape
+    Uo = np.empty_like(U)
+    Vo = np.empty_like(V)
+    lib().bmo_trilateral(_p(U), _p(V), _p(Um), _p(Vm), _p(I), sEPE2, sI2, sS2, sx, sy, _p(Uo), _p(Vo))
+    return Uo, Vo
+
+
+def refine(U, V, Iprev, fsize, sEPE, sI, sS):
+    U, V, Iprev = (_c(a, np.float32) for a in (U, V, Iprev))
+    sy, sx = U.shape
+    Um, Vm, Uo, Vo = (np.empty_like(U) for _ in range(4))
+    lib().bmo_refine(_p(U), _p(V), _p(Iprev), sx, sy, fsize, sEPE, sI, sS, _p(Um), _p(Vm), _p(Uo), _p(Vo))
+    return Um, Vm, Uo, Vo
+
+
+def epe(U, V, Ugt, Vgt):
+    U, V, Ugt, Vgt = (_c(a, np.float32) for a in (U, V, Ugt, Vgt))
+    return lib().bmo_epe(_p(U), _p(V), _p(Ugt), _p(Vgt), U.size)
+
+
+def normals(seed, count):
+    out = np.empty(count, np.float32)
+    lib().bmo_normals(seed, count, _p(out))
+    return out
+
+
+class Sequence:
+    """OFPipeline-style frame loop on the CPU (of_pipeline.cpp:241-333), in the
+    same order as the engine's bm_frame: the first frame primes, later frames
+    produce the flow from the previous frame.
+
+    ``up_images`` lets a caller supply the up-sampled frames (e.g. the engine's,
+    to take libm-vs-fast-math Lanczos differences out of a comparison);
+    ``normals_fn(call, n)`` supplies the random-search normals of call ``call``;
+    ``nn`` the device's down-sampling index tables (see ``downsample``)."""
+
+    def __init__(self, params: dict, pattern, normals_fn, nn=None):
+        self.p = dict(params)
+        self.nn = nn
+        self.pattern = np.ascontiguousarray(pattern, np.float32)
+        self.normals_fn = normals_fn
+        self.taps = gauss_taps(self.p["sigma"])
+        self.F1 = None
+        self.prev_in = None
+        self.NX = self.NY = None
+        self.first = True
+        self.calls = 0
+
+    def frame(self, frame_u8, up=None):
+        p = self.p
+        sx, sy, sxi, syi, N = p["sx"], p["sy"], p["sx_in"], p["sy_in"], p["N"]
+        cur_in = np.asarray(frame_u8, np.float32)
+        if up is None:
+            up = cur_in if (sx == sxi and sy == syi) else upsample(cur_in, sx, sy)
+        F2 = features(up, self.pattern, N)
+        out = None
+        if self.F1 is not None:
+            n = sx * sy
+            it = p["iterations"]
+            nrm = np.concatenate([np.asarray(self.normals_fn(self.calls + k, n), np.float32).ravel() for k in range(it)]) \
+                if it else np.zeros(2 * n, np.float32)
+            first = self.first or not p["tInit"]
+            NX, NY, H = match(self.F1, F2, sx, sy, N, it, p["jfMax"], p["doubleProp"], first, search_dist(sx), nrm,
+                              self.NX, self.NY)
+            self.calls += it
+            self.first = False
+            self.NX, self.NY, self.H = NX, NY, H
+            U, V = downsample(NX, NY, sx, sy, sxi, syi, self.taps, self.nn)
+            self.U, self.V = U, V
+            if p["filter"]:
+                Um, Vm, Uo, Vo = refine(U, V, self.prev_in, p["fsize"], p["sEPE"], p["sI"], p["sS"])
+                self.Um, self.Vm = Um, Vm
+                out = (Uo, Vo)
+            else:
+                out = (U, V)
+        self.F1 = F2
+        self.prev_in = cur_in
+        return out
