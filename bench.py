@@ -1,0 +1,454 @@
+#!/usr/bin/env python
+"""Throughput of the BriefMatch flow engine on GB300: output flow Mpx/s.
+
+Workload (one "step"): a seeded synthetic 8-frame 1024x436 8-bit sequence (7
+consecutive pairs, flow redrawn per pair, |v| <= 15 px), up-sampling 2.9x2.9,
+feature_length 128, FP32 flow output, temporal initialisation between pairs --
+the reference's "moderate" setting.  Synthetic frames stand in for the public
+benchmark sequences.
+
+  value    7 pairs * 1024*436 output pixels / device time per step (frames
+           already in HBM as uint8, outputs left in HBM); L2 flushed between steps
+  e2e      the same through the public C ABI with pinned host frames in and host
+           flow out (H2D and D2H inside the timed region)
+  roofline the dominant kernel's algorithmic bytes per launch over its mean
+           CUDA-event duration, against the measured HBM copy bandwidth
+  cpu_baseline  the oracle (scalar C + OpenMP transcription of the reference
+           kernels) on a bounded sample of the same workload, host cores
+
+`--impl reference` times the reference's own implementation of the path.  The
+reference has no CPU path, so its CPU-timed arm is the oracle transcription (all
+host threads), per the one-pair sample per step; the line also carries the
+reference's own CUDA kernels (compiled from its sources) timed on the GPU over
+the full step, when that build is present.
+
+Multi-GPU: one process per GPU (torchrun); each rank runs an independent
+replica on its own sequence (pairs shard with no exchange), value = all ranks'
+pixels / max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "output flow Mpx/s at fixed EPE: batched+learned-seeded vs plain, same GB300"
+UNIT = "Mpx/s"
+W, H, FRAMES, UP, NBITS, VMAX, SEED = 1024, 436, 8, 2.9, 128, 15.0, 20261203
+PAIRS = FRAMES - 1
+WORKLOAD = ("plain engine, synthetic 1024x436 8-bit sequence of 8 frames (7 pairs, |v|<=15 px), "
+            "up-sampling 2.9x2.9, feature_length 128, temporal init, FP32 flow out")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-pairs", type=int, default=2, help="pairs in the CPU-baseline sample")
+    return ap.parse_args()
+
+
+def dist_init(torch):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if torch.cuda.is_available():
+        torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    return world, rank
+
+
+def barrier(torch, world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(torch, world, v):
+    if world == 1:
+        return v
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.p:
+            time.sleep(0.25)
+            self.p.terminate()
+            try:
+                self.out, _ = self.p.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+                self.out = ""
+
+    def summary(self):
+        rows = [r.split(", ") for r in getattr(self, "out", "").strip().splitlines() if r.strip()]
+        rows = [r for r in rows if len(r) >= 9]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if "Active" in r[5 + k] and "Not" not in r[5 + k]})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "traffic_per_launch.txt")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        for line in f:
+            parts = line.split()
+            if len(parts) >= 2 and parts[0] == kernel:
+                try:
+                    return float(parts[1])
+                except ValueError:
+                    return None
+    return None
+
+
+def make_workload(rank):
+    from briefmatch_gb300 import synth
+
+    return synth.make_sequence(SEED + rank, W, H, FRAMES, vmax=VMAX)
+
+
+def algorithmic_bytes(kernel, prm):
+    """Bytes one launch must move at minimum (the per-unit figures in the design doc)."""
+    n = prm.sx * prm.sy
+    ni = prm.sx_in * prm.sy_in
+    ns = (prm.N + 31) // 32
+    cands = 4 if prm.doubleProp else 2
+    table = {
+        # per pixel: the candidates' descriptors gathered, the field read and written
+        # (4 B) and the cost read and written (2 B each)
+        "jump_level": n * (cands * ns * 4 + 2 * 4 + 2 * 2),
+        "jump_level_rs": n * ((cands + 1) * ns * 4 + 2 * 4 + 2 * 2),
+        # up-sampled image read once, descriptors written once
+        "features": n * (4 + ns * 4),
+        "initialize": n * (2 * ns * 4 + 4 + 2),
+        "upsample_u8": ni + n * 4,
+        # five float planes read, two written
+        "trilateral": ni * 7 * 4,
+        "median_pass": ni * 2 * 2 * 4,
+        "downsample": n * 4 + ni * 2 * 4,
+        "u8_to_f32": ni * 5,
+    }
+    return table.get(kernel)
+
+
+def run_engine(args, torch, world, rank):
+    import numpy as np
+
+    import briefmatch_gb300 as bm
+
+    frames, flows = make_workload(rank)
+    prm = bm.BMParams.derive(W, H, UP, UP, N=NBITS)
+    eng = bm.BriefMatch(prm)
+    eng.setup()
+    pattern = prm.make_pattern(SEED)
+    eng.set_pattern(pattern)
+    stream = torch.cuda.current_stream()
+    eng.set_stream(stream.cuda_stream)
+
+    d_frames = torch.from_numpy(np.stack(frames)).cuda()
+    d_u = torch.empty(PAIRS, H, W, device="cuda")
+    d_v = torch.empty(PAIRS, H, W, device="cuda")
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")  # > 129 MB L2
+
+    def step():
+        # every step is the same sequence from the same random-stream position
+        eng.reset_sequence()
+        eng.set_rng_position(0)
+        for k in range(FRAMES):
+            if k == 0:
+                eng.frame(d_frames[0].data_ptr(), True)
+            else:
+                eng.frame(d_frames[k].data_ptr(), True, d_u[k - 1].data_ptr(), d_v[k - 1].data_ptr(), True)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    # timed region: per-step CUDA events; L2 flushed before every step, outside the events
+    eng.profile(True)
+    eng.profile_reset()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    launches0 = eng.launch_count()
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        barrier(torch, world)
+        torch.cuda.synchronize()
+        for i in range(args.steps):
+            flush.zero_()
+            starts[i].record(stream)
+            step()
+            ends[i].record(stream)
+        torch.cuda.synchronize()
+        barrier(torch, world)
+    launches = eng.launch_count() - launches0
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_ms = max_over_ranks(torch, world, sum(step_ms))
+    kstats = eng.profile_read()
+    eng.profile(False)
+    ms_per_step = total_ms / args.steps
+    px_step = PAIRS * W * H
+    value = world * px_step / (ms_per_step * 1e-3) / 1e6
+
+    # accuracy of the last step
+    u = d_u.cpu().numpy()
+    v = d_v.cpu().numpy()
+    epes = [float(np.mean(np.hypot(u[k] - flows[k][0], v[k] - flows[k][1]))) for k in range(PAIRS)]
+
+    # end to end through the C ABI with pinned host buffers
+    h_frames = torch.from_numpy(np.stack(frames)).pin_memory()
+    h_u = torch.empty(PAIRS, H, W).pin_memory()
+    h_v = torch.empty(PAIRS, H, W).pin_memory()
+
+    def step_e2e():
+        eng.reset_sequence()
+        eng.set_rng_position(0)
+        for k in range(FRAMES):
+            if k == 0:
+                eng.frame(h_frames[0].data_ptr(), False)
+            else:
+                eng.frame(h_frames[k].data_ptr(), False, h_u[k - 1].data_ptr(), h_v[k - 1].data_ptr(), False)
+
+    for _ in range(max(1, args.warmup)):
+        step_e2e()
+    torch.cuda.synchronize()
+    e2e_ms = 0.0
+    barrier(torch, world)
+    for i in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        step_e2e()
+        torch.cuda.synchronize()
+        e2e_ms += (time.perf_counter() - t0) * 1e3
+    e2e_ms = max_over_ranks(torch, world, e2e_ms)
+    e2e_value = world * px_step / (e2e_ms / args.steps * 1e-3) / 1e6
+    assert np.array_equal(h_u.numpy(), u) and np.array_equal(h_v.numpy(), v), "host and device paths disagree"
+
+    # roofline of the dominant kernel (by total device time in the timed region)
+    dom = max(kstats.items(), key=lambda kv: kv[1][1])[0]
+    n_launch, dom_ms = kstats[dom]
+    per_launch_ms = dom_ms / n_launch
+    abytes = algorithmic_bytes(dom, prm)
+    peak, peak_src = measured_peaks()
+    achieved = abytes / (per_launch_ms * 1e-3) / 1e9 if abytes else None
+    total_k = sum(t for _, t in kstats.values())
+    roofline = {
+        "kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+        "frac": (achieved / peak) if achieved else None, "peak_source": peak_src + " (MEASURED_PEAKS.json hbm_gbs)",
+        "algorithmic_bytes_per_launch": abytes, "launch_ms": per_launch_ms, "launches": n_launch,
+        "share_of_kernel_time": dom_ms / total_k if total_k else None,
+        "traffic": ncu_traffic(dom),
+    }
+    kernels = {k: {"launches": c, "ms": round(t, 4), "share": round(t / total_k, 4)} for k, (c, t) in
+               sorted(kstats.items(), key=lambda kv: -kv[1][1])}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(prm, pattern, frames, args.cpu_pairs)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u32 descriptors / int16 field / f32 flow", "data": "synthetic (seeded generator; see bench.py)",
+        "config": {"workload": WORKLOAD, "width": W, "height": H, "frames_per_step": FRAMES, "pairs_per_step": PAIRS,
+                   "upsampling": UP, "feature_length": NBITS, "grid": [prm.sx, prm.sy], "iterations": prm.iterations,
+                   "jfMax": prm.jfMax, "fsize": prm.fsize, "l2": "flushed (256 MB write) before every timed step",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "epe": {"mean": float(np.mean(epes)), "per_pair": [round(e, 4) for e in epes]},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(FRAMES * W * H),
+                "d2h_bytes_per_step": int(PAIRS * 2 * W * H * 4)},
+        "gpu_launches": int(launches),
+        "clocks": clk.summary(),
+        "roofline": roofline,
+        "kernels": kernels,
+        "cpu_baseline": cpu,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    eng.clean()
+
+
+def cpu_baseline(prm, pattern, frames, pairs):
+    """The oracle over `pairs` pairs of the workload on all host threads."""
+    import numpy as np
+
+    import oracle
+
+    nt = oracle.num_threads()
+    p = prm.as_dict()
+    n = prm.sx * prm.sy
+    seq = oracle.Sequence(p, pattern, lambda call, cnt: oracle.normals(1000 + call, 2 * cnt))
+    seq.frame(frames[0])
+    t0 = time.perf_counter()
+    for k in range(1, pairs + 1):
+        seq.frame(frames[k])
+    dt = time.perf_counter() - t0
+    return {"value": pairs * W * H / dt / 1e6, "unit": UNIT, "cores": nt, "kind": "port",
+            "sample": "%d consecutive pair(s) of the 1024x436 sequence (after priming frame 0), %.1f s" % (pairs, dt)}
+
+
+def run_reference(args, torch, world, rank):
+    """The reference's own implementation of the path.  Only rank 0 works."""
+    if rank != 0:
+        return
+    import numpy as np
+
+    import briefmatch_gb300 as bm
+    import oracle
+
+    frames, flows = make_workload(rank)
+    prm = bm.BMParams.derive(W, H, UP, UP, N=NBITS)
+    pattern = prm.make_pattern(SEED)
+    nt = oracle.num_threads()
+    p = prm.as_dict()
+    seq = oracle.Sequence(p, pattern, lambda call, cnt: oracle.normals(1000 + call, 2 * cnt))
+    k = 0
+    seq.frame(frames[0])
+
+    def one_pair():
+        nonlocal k
+        k += 1
+        if k >= FRAMES:
+            seq.__init__(p, pattern, seq.normals_fn)
+            seq.frame(frames[0])
+            k = 1
+        t0 = time.perf_counter()
+        seq.frame(frames[k])
+        return time.perf_counter() - t0
+
+    for _ in range(args.warmup):
+        one_pair()
+    times = [one_pair() for _ in range(args.steps)]
+    tot = sum(times)
+    value = args.steps * W * H / tot / 1e6
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": tot / args.steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "impl": "reference", "dtype": "u32 descriptors / int16 field / f32 flow",
+        "data": "synthetic (seeded generator; see bench.py)",
+        "config": {"workload": WORKLOAD, "width": W, "height": H, "upsampling": UP, "feature_length": NBITS,
+                   "step": "one pair of the sequence per step (bounded CPU sample)"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nt, "kind": "port",
+                         "sample": "one pair per step of the 1024x436 sequence, %d threads" % nt},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    try:
+        line["reference_cuda_build"] = reference_cuda(torch, prm, pattern, frames, args)
+    except Exception as e:  # the reference kernel build is optional
+        line["reference_cuda_build"] = {"unavailable": str(e)[:200]}
+    print(json.dumps(line), flush=True)
+
+
+def reference_cuda(torch, prm, pattern, frames, args):
+    """The reference's kernels (compiled from its sources) over the full step on the GPU."""
+    import numpy as np
+
+    from oracle import refshim
+
+    if not torch.cuda.is_available():
+        return {"unavailable": "no GPU"}
+    if not refshim.available():
+        return {"unavailable": "reference kernel build (oracle/_ref) not present"}
+    pipe = refshim.RefPipeline(torch, prm.as_dict(), pattern, prm.gauss_taps())
+    d_frames = [torch.from_numpy(f.astype(np.float32)).cuda() for f in frames]
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+
+    def step():
+        pipe.primed = False
+        pipe.first = True
+        for f in d_frames:
+            pipe.frame(f)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    tot = 0.0
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        s = torch.cuda.Event(enable_timing=True)
+        e = torch.cuda.Event(enable_timing=True)
+        s.record()
+        step()
+        e.record()
+        torch.cuda.synchronize()
+        tot += s.elapsed_time(e)
+    ms = tot / args.steps
+    return {"value": PAIRS * W * H / (ms * 1e-3) / 1e6, "unit": UNIT, "ms_per_step": ms,
+            "how": "reference kernels/briefmatch_cuda.cu + util_cuda.cu compiled unmodified (-O3 -use_fast_math, "
+                   "sm_103a), launched with the reference's 32x32 blocks and a device sync after every launch"}
+
+
+def main():
+    args = parse()
+    import torch
+
+    world, rank = dist_init(torch)
+    if args.impl == "reference":
+        run_reference(args, torch, world, rank)
+    else:
+        run_engine(args, torch, world, rank)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -39,6 +39,10 @@ class CudaException(RuntimeError):
     """CUDA runtime errors (util_cuda.h:85-100)."""
 
 
+class bm_kernel_stat(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char_p), ("launches", ctypes.c_uint64), ("ms", ctypes.c_double)]
+
+
 class bm_params(ctypes.Structure):
     _fields_ = [
         ("sx", ctypes.c_uint32), ("sy", ctypes.c_uint32), ("sx_in", ctypes.c_uint32), ("sy_in", ctypes.c_uint32),
@@ -96,6 +100,9 @@ def _declare(lib):
         "bm_frame": (c.c_int, [c.c_void_p, c.c_void_p, c.c_int, c.c_void_p, c.c_void_p, c.c_int]),
         "bm_reset_sequence": (c.c_int, [c.c_void_p]),
         "bm_launch_count": (c.c_uint64, [c.c_void_p]),
+        "bm_profile_enable": (c.c_int, [c.c_void_p, c.c_int]),
+        "bm_profile_reset": (c.c_int, [c.c_void_p]),
+        "bm_profile_read": (c.c_int, [c.c_void_p, c.c_void_p, c.c_uint32, P(c.c_uint32)]),
         "bm_last_error": (c.c_char_p, []),
         "bm_version": (c.c_char_p, []),
     }
@@ -325,6 +332,20 @@ class BriefMatch:
 
     def launch_count(self):
         return int(lib().bm_launch_count(self.ctx))
+
+    def profile(self, on=True):
+        check(lib().bm_profile_enable(self.ctx, int(bool(on))))
+
+    def profile_reset(self):
+        check(lib().bm_profile_reset(self.ctx))
+
+    def profile_read(self):
+        """{kernel name: (launches, total ms)} since the last reset (synchronises)."""
+        n = ctypes.c_uint32(0)
+        check(lib().bm_profile_read(self.ctx, None, 0, ctypes.byref(n)))
+        arr = (bm_kernel_stat * max(1, n.value))()
+        check(lib().bm_profile_read(self.ctx, arr, n.value, ctypes.byref(n)))
+        return {arr[i].name.decode(): (int(arr[i].launches), float(arr[i].ms)) for i in range(n.value)}
 
 
 class FlowEngine(BriefMatch):

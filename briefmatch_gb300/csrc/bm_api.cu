@@ -38,10 +38,15 @@ bm_status fail(bm_status st, const char* fmt, ...)
                         __LINE__);                                                           \
     } while (0)
 
-#define BM_LAUNCH(ctx, call)   \
-    do {                       \
-        BM_CUDA(call);         \
-        (ctx)->launches++;     \
+// Every kernel launch goes through BM_LAUNCH: it counts launches and, while
+// profiling is on, brackets the launch with CUDA events on the context's stream.
+#define BM_LAUNCH(ctx, name, call)                               \
+    do {                                                         \
+        cudaEvent_t a_ = nullptr, b_ = nullptr;                  \
+        if ((ctx)->prof_on) prof_begin((ctx), &a_, &b_);         \
+        BM_CUDA(call);                                           \
+        (ctx)->launches++;                                       \
+        if ((ctx)->prof_on) prof_end((ctx), (name), a_, b_);     \
     } while (0)
 
 }  // namespace
@@ -83,11 +88,75 @@ struct bm_ctx {
     bool primed = false;
     uint64_t launches = 0;
 
+    struct ProfRec {
+        const char* name;
+        cudaEvent_t a, b;
+    };
+    struct ProfTotal {
+        const char* name;
+        uint64_t launches;
+        double ms;
+    };
+    bool prof_on = false;
+    std::vector<ProfRec> prof_pending;
+    std::vector<cudaEvent_t> prof_pool;
+    std::vector<ProfTotal> prof_totals;
+
     uint32_t* feat1_ptr() const { return d_feat[feat1]; }
     uint32_t* feat2_ptr() const { return d_feat[feat1 ^ 1]; }
 };
 
 namespace {
+
+cudaEvent_t prof_event(bm_ctx* c)
+{
+    if (!c->prof_pool.empty()) {
+        cudaEvent_t e = c->prof_pool.back();
+        c->prof_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+    return e;
+}
+
+void prof_begin(bm_ctx* c, cudaEvent_t* a, cudaEvent_t* b)
+{
+    *a = prof_event(c);
+    *b = prof_event(c);
+    if (*a) cudaEventRecord(*a, c->stream);
+}
+
+void prof_end(bm_ctx* c, const char* name, cudaEvent_t a, cudaEvent_t b)
+{
+    if (!a || !b) return;
+    cudaEventRecord(b, c->stream);
+    c->prof_pending.push_back({name, a, b});
+}
+
+// Fold finished launch records into the per-kernel totals (synchronises the stream).
+cudaError_t prof_collect(bm_ctx* c)
+{
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return e;
+    for (auto& r : c->prof_pending) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, r.a, r.b);
+        bool found = false;
+        for (auto& t : c->prof_totals)
+            if (std::strcmp(t.name, r.name) == 0) {
+                t.launches++;
+                t.ms += ms;
+                found = true;
+                break;
+            }
+        if (!found) c->prof_totals.push_back({r.name, 1, (double)ms});
+        c->prof_pool.push_back(r.a);
+        c->prof_pool.push_back(r.b);
+    }
+    c->prof_pending.clear();
+    return cudaSuccess;
+}
 
 template <typename T>
 bm_status dev_alloc(T** p, size_t count)
@@ -110,6 +179,11 @@ void release(bm_ctx* c)
                     c->d_nnx, c->d_nny};
     for (void* p : ptrs)
         if (p) cudaFree(p);
+    for (auto& r : c->prof_pending) {
+        cudaEventDestroy(r.a);
+        cudaEventDestroy(r.b);
+    }
+    for (cudaEvent_t e : c->prof_pool) cudaEventDestroy(e);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
 }
 
@@ -133,7 +207,7 @@ bmk::RsArgs rs_args(const bm_ctx* c, bool enabled)
 bm_status features_into(bm_ctx* c, const float* d_up, uint32_t* F)
 {
     const bm_params& p = c->prm;
-    BM_LAUNCH(c, bmk::features(d_up, F, (int)p.sx, (int)p.sy, (int)p.N, (int)c->nsp, c->d_pattern, c->pattern_rmax,
+    BM_LAUNCH(c, "features", bmk::features(d_up, F, (int)p.sx, (int)p.sy, (int)p.N, (int)c->nsp, c->d_pattern, c->pattern_rmax,
                                c->stream));
     return BM_OK;
 }
@@ -149,7 +223,7 @@ bm_status propagate_pass(bm_ctx* c, int pd, bool fuse_rs)
     for (int step = (int)p.jfMax; step > 0; step /= 2, lvl++) {
         const bool last = (lvl == levels - 1);
         bmk::RsArgs rs = rs_args(c, fuse_rs && last);
-        BM_LAUNCH(c, bmk::jump_level(c->feat1_ptr(), c->feat2_ptr(), c->d_flow[c->flow_cur], c->d_flow[c->flow_cur ^ 1],
+        BM_LAUNCH(c, rs.enabled ? "jump_level_rs" : "jump_level", bmk::jump_level(c->feat1_ptr(), c->feat2_ptr(), c->d_flow[c->flow_cur], c->d_flow[c->flow_cur ^ 1],
                                      c->d_cost, (int)p.sx, (int)p.sy, (int)c->nsp, step, pd, p.doubleProp ? 1 : 0, rs,
                                      c->stream));
         c->flow_cur ^= 1;
@@ -157,7 +231,7 @@ bm_status propagate_pass(bm_ctx* c, int pd, bool fuse_rs)
     if (fuse_rs) {
         if (levels == 0) {
             bmk::RsArgs rs = rs_args(c, true);
-            BM_LAUNCH(c, bmk::random_search(c->feat1_ptr(), c->feat2_ptr(), c->d_flow[c->flow_cur], c->d_cost, (int)p.sx,
+            BM_LAUNCH(c, "random_search", bmk::random_search(c->feat1_ptr(), c->feat2_ptr(), c->d_flow[c->flow_cur], c->d_cost, (int)p.sx,
                                             (int)p.sy, (int)c->nsp, rs, c->stream));
         }
         c->rs_calls++;
@@ -171,7 +245,7 @@ bm_status match_impl(bm_ctx* c, const float* d_im2)
     bm_status st = features_into(c, d_im2, c->feat2_ptr());
     if (st != BM_OK) return st;
     const int first = (c->first_match || !p.tInit) ? 1 : 0;
-    BM_LAUNCH(c, bmk::initialize(c->feat1_ptr(), c->feat2_ptr(), c->d_flow[c->flow_cur], c->d_flow[c->flow_cur ^ 1],
+    BM_LAUNCH(c, "initialize", bmk::initialize(c->feat1_ptr(), c->feat2_ptr(), c->d_flow[c->flow_cur], c->d_flow[c->flow_cur ^ 1],
                                  c->d_cost, (int)p.sx, (int)p.sy, (int)c->nsp, first, c->stream));
     c->flow_cur ^= 1;
     int pd = -1;
@@ -192,11 +266,11 @@ bm_status downsample_impl(bm_ctx* c)
     if (p.sx_in != p.sx || p.sy_in != p.sy) {
         const float mx = (float)p.sx_in / (float)p.sx;  // briefmatch.cpp:316-317
         const float my = (float)p.sy_in / (float)p.sy;
-        BM_LAUNCH(c, bmk::downsample(c->d_flow[c->flow_cur], U, V, (int)p.sx, (int)p.sy, (int)p.sx_in, (int)p.sy_in,
+        BM_LAUNCH(c, "downsample", bmk::downsample(c->d_flow[c->flow_cur], U, V, (int)p.sx, (int)p.sy, (int)p.sx_in, (int)p.sy_in,
                                      c->d_taps, (int)p.P, mx, my, c->d_nnx, c->d_nny, c->stream));
     } else {
         // briefmatch.cpp:319-323: the converted field is the output
-        BM_LAUNCH(c, bmk::flow_to_planes(c->d_flow[c->flow_cur], U, V, c->npix, c->stream));
+        BM_LAUNCH(c, "flow_to_planes", bmk::flow_to_planes(c->d_flow[c->flow_cur], U, V, c->npix, c->stream));
     }
     return BM_OK;
 }
@@ -210,10 +284,10 @@ bm_status process_impl(bm_ctx* c, const float* d_prev_in)
     if (p.filter) {
         if (!d_prev_in) return fail(BM_ERR_INVALID, "process: the guide frame is required when filtering");
         const int fs = p.fsize == 0 ? 1 : (int)p.fsize;
-        BM_LAUNCH(c, bmk::median_pass(U, V, c->d_tmp, c->d_tmp + n, 1, fs, (int)p.sx_in, (int)p.sy_in, c->stream));
-        BM_LAUNCH(c, bmk::median_pass(c->d_tmp, c->d_tmp + n, c->d_flow_med, c->d_flow_med + n, 0, fs, (int)p.sx_in,
+        BM_LAUNCH(c, "median_pass", bmk::median_pass(U, V, c->d_tmp, c->d_tmp + n, 1, fs, (int)p.sx_in, (int)p.sy_in, c->stream));
+        BM_LAUNCH(c, "median_pass", bmk::median_pass(c->d_tmp, c->d_tmp + n, c->d_flow_med, c->d_flow_med + n, 0, fs, (int)p.sx_in,
                                       (int)p.sy_in, c->stream));
-        BM_LAUNCH(c, bmk::trilateral(U, V, c->d_flow_med, c->d_flow_med + n, d_prev_in, c->d_flow_out,
+        BM_LAUNCH(c, "trilateral", bmk::trilateral(U, V, c->d_flow_med, c->d_flow_med + n, d_prev_in, c->d_flow_out,
                                      c->d_flow_out + n, (int)p.sx_in, (int)p.sy_in, c->tri_s, p.sEPE * p.sEPE,
                                      p.sI * p.sI, p.sS * p.sS, c->stream));
     } else {
@@ -464,7 +538,7 @@ bm_status bm_upsample(bm_ctx* c, const float* d_in, float* d_out)
     if (check_ctx(c)) return BM_ERR_INVALID;
     if (!d_in || !d_out) return fail(BM_ERR_INVALID, "bm_upsample: null buffer");
     const bm_params& p = c->prm;
-    BM_LAUNCH(c, bmk::upsample_f32(d_in, d_out, (int)p.sx_in, (int)p.sy_in, (int)p.sx, (int)p.sy, c->d_lx, c->d_ix,
+    BM_LAUNCH(c, "upsample_f32", bmk::upsample_f32(d_in, d_out, (int)p.sx_in, (int)p.sy_in, (int)p.sx, (int)p.sy, c->d_lx, c->d_ix,
                                    c->d_ly, c->d_iy, c->stream));
     return BM_OK;
 }
@@ -474,7 +548,7 @@ bm_status bm_upsample_u8(bm_ctx* c, const uint8_t* d_in, float* d_out)
     if (check_ctx(c)) return BM_ERR_INVALID;
     if (!d_in || !d_out) return fail(BM_ERR_INVALID, "bm_upsample_u8: null buffer");
     const bm_params& p = c->prm;
-    BM_LAUNCH(c, bmk::upsample_u8(d_in, d_out, (int)p.sx_in, (int)p.sy_in, (int)p.sx, (int)p.sy, c->d_lx, c->d_ix,
+    BM_LAUNCH(c, "upsample_u8", bmk::upsample_u8(d_in, d_out, (int)p.sx_in, (int)p.sy_in, (int)p.sx, (int)p.sy, c->d_lx, c->d_ix,
                                   c->d_ly, c->d_iy, c->stream));
     return BM_OK;
 }
@@ -491,7 +565,7 @@ bm_status bm_initialize(bm_ctx* c, int first)
 {
     if (check_ctx(c)) return BM_ERR_INVALID;
     const bm_params& p = c->prm;
-    BM_LAUNCH(c, bmk::initialize(c->feat1_ptr(), c->feat2_ptr(), c->d_flow[c->flow_cur], c->d_flow[c->flow_cur ^ 1],
+    BM_LAUNCH(c, "initialize", bmk::initialize(c->feat1_ptr(), c->feat2_ptr(), c->d_flow[c->flow_cur], c->d_flow[c->flow_cur ^ 1],
                                  c->d_cost, (int)p.sx, (int)p.sy, (int)c->nsp, first ? 1 : 0, c->stream));
     c->flow_cur ^= 1;
     return BM_OK;
@@ -508,7 +582,7 @@ bm_status bm_random_search(bm_ctx* c)
     if (check_ctx(c)) return BM_ERR_INVALID;
     const bm_params& p = c->prm;
     bmk::RsArgs rs = rs_args(c, true);
-    BM_LAUNCH(c, bmk::random_search(c->feat1_ptr(), c->feat2_ptr(), c->d_flow[c->flow_cur], c->d_cost, (int)p.sx,
+    BM_LAUNCH(c, "random_search", bmk::random_search(c->feat1_ptr(), c->feat2_ptr(), c->d_flow[c->flow_cur], c->d_cost, (int)p.sx,
                                     (int)p.sy, (int)c->nsp, rs, c->stream));
     c->rs_calls++;
     return BM_OK;
@@ -555,7 +629,7 @@ bm_status bm_convert(bm_ctx* c, float* h_u, float* h_v)
 bm_status bm_export_field(bm_ctx* c, int16_t* d_nx, int16_t* d_ny, float* d_dist)
 {
     if (check_ctx(c)) return BM_ERR_INVALID;
-    BM_LAUNCH(c, bmk::export_field(c->d_flow[c->flow_cur], c->d_cost, d_nx, d_ny, d_dist, c->npix, (int)c->prm.N,
+    BM_LAUNCH(c, "export_field", bmk::export_field(c->d_flow[c->flow_cur], c->d_cost, d_nx, d_ny, d_dist, c->npix, (int)c->prm.N,
                                    c->stream));
     return BM_OK;
 }
@@ -564,7 +638,7 @@ bm_status bm_import_field(bm_ctx* c, const int16_t* d_nx, const int16_t* d_ny, c
 {
     if (check_ctx(c)) return BM_ERR_INVALID;
     if (!d_nx || !d_ny) return fail(BM_ERR_INVALID, "bm_import_field: null field");
-    BM_LAUNCH(c, bmk::import_field(d_nx, d_ny, d_cost, c->d_flow[c->flow_cur], c->d_cost, c->npix, c->stream));
+    BM_LAUNCH(c, "import_field", bmk::import_field(d_nx, d_ny, d_cost, c->d_flow[c->flow_cur], c->d_cost, c->npix, c->stream));
     return BM_OK;
 }
 
@@ -574,7 +648,7 @@ bm_status bm_normals(bm_ctx* c, uint64_t call, float* d_out)
     if (!d_out) return fail(BM_ERR_INVALID, "bm_normals: null output");
     bmk::RsArgs rs = rs_args(c, true);
     rs.call = call;
-    BM_LAUNCH(c, bmk::normals(reinterpret_cast<float2*>(d_out), (int)c->prm.sx, (int)c->prm.sy, rs, c->stream));
+    BM_LAUNCH(c, "normals", bmk::normals(reinterpret_cast<float2*>(d_out), (int)c->prm.sx, (int)c->prm.sy, rs, c->stream));
     return BM_OK;
 }
 
@@ -612,6 +686,36 @@ bm_status bm_reset_sequence(bm_ctx* c)
 
 uint64_t bm_launch_count(const bm_ctx* c) { return c ? c->launches : 0; }
 
+bm_status bm_profile_enable(bm_ctx* c, int on)
+{
+    if (check_ctx(c)) return BM_ERR_INVALID;
+    c->prof_on = on != 0;
+    return BM_OK;
+}
+
+bm_status bm_profile_reset(bm_ctx* c)
+{
+    if (check_ctx(c)) return BM_ERR_INVALID;
+    BM_CUDA(prof_collect(c));
+    c->prof_totals.clear();
+    return BM_OK;
+}
+
+bm_status bm_profile_read(bm_ctx* c, bm_kernel_stat* out, uint32_t cap, uint32_t* count)
+{
+    if (check_ctx(c)) return BM_ERR_INVALID;
+    if (!count) return fail(BM_ERR_INVALID, "bm_profile_read: null count");
+    BM_CUDA(prof_collect(c));
+    *count = (uint32_t)c->prof_totals.size();
+    if (out)
+        for (uint32_t i = 0; i < cap && i < *count; i++) {
+            out[i].name = c->prof_totals[i].name;
+            out[i].launches = c->prof_totals[i].launches;
+            out[i].ms = c->prof_totals[i].ms;
+        }
+    return BM_OK;
+}
+
 bm_status bm_frame(bm_ctx* c, const uint8_t* frame, int frame_on_device, float* u, float* v, int out_on_device)
 {
     if (check_ctx(c)) return BM_ERR_INVALID;
@@ -625,11 +729,11 @@ bm_status bm_frame(bm_ctx* c, const uint8_t* frame, int frame_on_device, float* 
         d_u8 = c->d_frame_u8;
     }
     float* cur = c->d_frame[c->cur_frame];
-    BM_LAUNCH(c, bmk::u8_to_f32(d_u8, cur, ni, c->stream));
+    BM_LAUNCH(c, "u8_to_f32", bmk::u8_to_f32(d_u8, cur, ni, c->stream));
     // of_pipeline.cpp:301-310
     const float* up = cur;
     if (p.sx != p.sx_in || p.sy != p.sy_in) {
-        BM_LAUNCH(c, bmk::upsample_u8(d_u8, c->d_up, (int)p.sx_in, (int)p.sy_in, (int)p.sx, (int)p.sy, c->d_lx, c->d_ix,
+        BM_LAUNCH(c, "upsample_u8", bmk::upsample_u8(d_u8, c->d_up, (int)p.sx_in, (int)p.sy_in, (int)p.sx, (int)p.sy, c->d_lx, c->d_ix,
                                       c->d_ly, c->d_iy, c->stream));
         up = c->d_up;
     }

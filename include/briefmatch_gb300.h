@@ -210,6 +210,19 @@ bm_status bm_reset_sequence(bm_ctx* ctx);
 /* Count of kernels this context has launched (for launch accounting). */
 uint64_t bm_launch_count(const bm_ctx* ctx);
 
+/* Per-kernel device time (the reference's CudaTimer, util_cuda.cu:287-313, per
+ * launch instead of per stage).  While enabled, every launch is bracketed by CUDA
+ * events on the context's stream; bm_profile_read synchronises the stream and
+ * returns one entry per kernel name (name, launches, total milliseconds). */
+typedef struct bm_kernel_stat {
+    const char* name;
+    uint64_t launches;
+    double ms;
+} bm_kernel_stat;
+bm_status bm_profile_enable(bm_ctx* ctx, int on);
+bm_status bm_profile_reset(bm_ctx* ctx);
+bm_status bm_profile_read(bm_ctx* ctx, bm_kernel_stat* out, uint32_t cap, uint32_t* count);
+
 const char* bm_last_error(void);
 const char* bm_version(void);
 

@@ -125,3 +125,87 @@ def guarded(torch, n, guard, dtype, device="cuda"):
     returns (storage, body view)."""
     store = torch.zeros(n + 2 * guard, dtype=dtype, device=device)
     return store, store[guard:guard + n]
+
+
+class RefPipeline:
+    """OFPipeline::processFrame + BriefMatch::match/downsample/process
+    (of_pipeline.cpp:296-333, briefmatch.cpp:248-352) driven through the
+    reference's own kernels, for timing the reference build on the GPU.
+
+    Frames are float input-resolution device tensors (the reference uploads
+    float, of_pipeline.cpp:297).  The first frame primes (descriptors only), as
+    the engine does; later frames run the full pair.  Buffers the reference
+    reads out of bounds carry zero guard bands."""
+
+    def __init__(self, torch, params: dict, pattern, taps):
+        self.t = torch
+        self.k = RefKernels()
+        p = self.p = dict(params)
+        self.k.set_pattern(pattern)
+        self.k.set_kernel(taps)
+        self.P = len(taps)
+        sx, sy, sxi, syi = p["sx"], p["sy"], p["sx_in"], p["sy_in"]
+        n, ni = sx * sy, sxi * syi
+        self.ns = (p["N"] + 31) // 32
+        g = (p["jfMax"] + 1) * sx + p["jfMax"]
+        gm = (p["fsize"] // 2 + 1) * sxi + p["fsize"]
+        z = lambda cnt, dt=torch.float32: torch.zeros(cnt, dtype=dt, device="cuda")
+        self.L = z(n)
+        self.F = [z(n * self.ns, torch.int32), z(n * self.ns, torch.int32)]
+        self.D = z(n)
+        self._nx_store, self.NX = guarded(torch, n, g, torch.int16)
+        self._ny_store, self.NY = guarded(torch, n, g, torch.int16)
+        self.XF, self.YF, self.tmp = z(n), z(n), z(n)
+        self.state = z(n * CURAND_STATE_BYTES, torch.uint8)
+        self._xi, self.XI = guarded(torch, ni, gm, torch.float32)
+        self._yi, self.YI = guarded(torch, ni, gm, torch.float32)
+        self._ti, self.TI = guarded(torch, ni, gm, torch.float32)
+        self.XM, self.YM, self.XO, self.YO = z(ni), z(ni), z(ni), z(ni)
+        self.k.init_random(self.state.data_ptr(), sx, sy)
+        self.dist = float(np.sqrt(np.ceil(np.float32(sx) * np.float32(0.5) / np.float32(3.0)), dtype=np.float32))
+        self.first = True
+        self.primed = False
+        self.prev_in = None
+
+    def frame(self, d_in):
+        p, k = self.p, self.k
+        sx, sy, sxi, syi, N, ns = p["sx"], p["sy"], p["sx_in"], p["sy_in"], p["N"], self.ns
+        F1, F2 = self.F
+        if sx != sxi or sy != syi:
+            k.resize_lanczos(d_in.data_ptr(), self.L.data_ptr(), sxi, syi, sx, sy)
+            L = self.L
+        else:
+            L = d_in
+        k.binary_features(L.data_ptr(), F2.data_ptr(), sx, sy, N, ns)
+        if self.primed:
+            k.initialize(F1.data_ptr(), F2.data_ptr(), self.D.data_ptr(), self.NX.data_ptr(), self.NY.data_ptr(), sx, sy,
+                         self.first or not p["tInit"], N, ns)
+            pd = -1
+            for _ in range(p["iterations"]):
+                k.propagate(F1.data_ptr(), F2.data_ptr(), self.D.data_ptr(), self.NX.data_ptr(), self.NY.data_ptr(), sx, sy,
+                            pd, p["jfMax"], p["doubleProp"], N, ns)
+                k.random_search(F1.data_ptr(), F2.data_ptr(), self.D.data_ptr(), self.NX.data_ptr(), self.NY.data_ptr(),
+                                self.state.data_ptr(), sx, sy, self.dist, N, ns)
+                pd = -pd
+            self.first = False
+            k.convert(self.NX.data_ptr(), self.XF.data_ptr(), sx, sy)
+            k.convert(self.NY.data_ptr(), self.YF.data_ptr(), sx, sy)
+            if sx != sxi or sy != syi:
+                for F in (self.XF, self.YF):
+                    k.filter_const(F.data_ptr(), self.tmp.data_ptr(), self.P, 1, sx, sy)
+                    k.filter_const(self.tmp.data_ptr(), F.data_ptr(), self.P, 0, sx, sy)
+                k.resize_nn(self.XF.data_ptr(), self.XI.data_ptr(), sx, sy, sxi, syi)
+                k.resize_nn(self.YF.data_ptr(), self.YI.data_ptr(), sx, sy, sxi, syi)
+                k.mult(self.XI.data_ptr(), float(np.float32(sxi) / np.float32(sx)), sxi, syi)
+                k.mult(self.YI.data_ptr(), float(np.float32(syi) / np.float32(sy)), sxi, syi)
+            if p["filter"]:
+                k.median(self.XI.data_ptr(), self.TI.data_ptr(), 1, p["fsize"], sxi, syi)
+                k.median(self.TI.data_ptr(), self.XM.data_ptr(), 0, p["fsize"], sxi, syi)
+                k.median(self.YI.data_ptr(), self.TI.data_ptr(), 1, p["fsize"], sxi, syi)
+                k.median(self.TI.data_ptr(), self.YM.data_ptr(), 0, p["fsize"], sxi, syi)
+                k.cb_filter(self.XI.data_ptr(), self.YI.data_ptr(), self.XO.data_ptr(), self.YO.data_ptr(),
+                            self.XM.data_ptr(), self.YM.data_ptr(), self.prev_in.data_ptr(),
+                            p["sEPE"] * p["sEPE"], p["sI"] * p["sI"], p["sS"] * p["sS"], sxi, syi)
+        self.primed = True
+        self.F.reverse()
+        self.prev_in = d_in
