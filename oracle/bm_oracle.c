@@ -10,6 +10,7 @@
  */
 #include "bm_oracle.h"
 
+#include <float.h>
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
@@ -21,6 +22,13 @@
 static const double BMO_PI = 3.141592653589793115997963468544;
 
 static inline int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+/* The reference kernels are built with -use_fast_math, which implies flush-to-zero:
+ * single-precision operands and results below the smallest normal float are read
+ * and written as (sign-preserving) zero.  The bit-exact pieces apply the same rule. */
+static inline float ftzf(float v) { return fabsf(v) < FLT_MIN ? copysignf(0.0f, v) : v; }
+static inline float fma_ftz(float a, float b, float c) { return ftzf(fmaf(ftzf(a), ftzf(b), ftzf(c))); }
+static inline float mul_ftz(float a, float b) { return ftzf(ftzf(a) * ftzf(b)); }
 
 int bmo_num_threads(void)
 {
@@ -288,13 +296,14 @@ static inline float gauss_h(const int16_t* L, int sx, int x, int y, const float*
 {
     int ks2 = P / 2;
     float s = 0;
-    for (int i = 0; i < P; i++) s = fmaf(taps[i], (float)L[clampi(x + i - ks2, 0, sx - 1) + (size_t)y * sx], s);
+    for (int i = 0; i < P; i++) s = fma_ftz(taps[i], (float)L[clampi(x + i - ks2, 0, sx - 1) + (size_t)y * sx], s);
     return s;
 }
 
 /* briefmatch.cpp:296-324: int16 -> float (util_cuda.cu:174-183), Gaussian H then V
  * (util_cuda.cu:48-73), nearest-neighbour decimation (util_cuda.cu:160-172) and
- * scaling by sx_in/sx (util_cuda.cu:113-124).  Only the decimated pixels are
+ * scaling by sx_in/sx (util_cuda.cu:113-124), with flush-to-zero arithmetic.  Only
+ * the decimated pixels are
  * evaluated; each one repeats the reference's per-pass rounding.  The source index
  * round(x*sx/sx_in) is computed on the device with the fast-math division; where
  * that quotient lands exactly on .5 the IEEE quotient used here can round the other
@@ -328,11 +337,11 @@ void bmo_downsample(const int16_t* NX, const int16_t* NY, int sx, int sy,
             float su = 0, sv = 0;
             for (int i = 0; i < P; i++) {
                 int yy = clampi((int)y1 + i - ks2, 0, sy - 1);
-                su = fmaf(taps[i], gauss_h(NX, sx, (int)x1, yy, taps, P), su);
-                sv = fmaf(taps[i], gauss_h(NY, sx, (int)x1, yy, taps, P), sv);
+                su = fma_ftz(taps[i], gauss_h(NX, sx, (int)x1, yy, taps, P), su);
+                sv = fma_ftz(taps[i], gauss_h(NY, sx, (int)x1, yy, taps, P), sv);
             }
-            U[o] = su * mx;
-            V[o] = sv * my;
+            U[o] = mul_ftz(su, mx);
+            V[o] = mul_ftz(sv, my);
         }
     }
 }
