@@ -73,6 +73,7 @@ struct bm_ctx {
     float* d_tmp = nullptr;
     int4* d_pattern = nullptr;
     int pattern_rmax = 0;
+    bmk::PatternOffsets pattern_off;   // linear offsets for width sx
     float* d_taps = nullptr;
     float* d_lx = nullptr;
     int* d_ix = nullptr;
@@ -208,7 +209,7 @@ bm_status features_into(bm_ctx* c, const float* d_up, uint32_t* F)
 {
     const bm_params& p = c->prm;
     BM_LAUNCH(c, "features", bmk::features(d_up, F, (int)p.sx, (int)p.sy, (int)p.N, (int)c->nsp, c->d_pattern, c->pattern_rmax,
-                               c->stream));
+                               c->pattern_off, c->stream));
     return BM_OK;
 }
 
@@ -310,6 +311,10 @@ bm_status set_pattern_impl(bm_ctx* c, const float* h_pattern)
         }
         pat[s] = make_int4(v[0], v[1], v[2], v[3]);
     }
+    std::memset(&c->pattern_off, 0, sizeof(c->pattern_off));
+    const int sx = (int)c->prm.sx;
+    for (uint32_t s = 0; s < N; s++)
+        c->pattern_off.off[s] = make_int2(pat[s].x + pat[s].y * sx, pat[s].z + pat[s].w * sx);
     BM_CUDA(cudaMemcpyAsync(c->d_pattern, pat.data(), N * sizeof(int4), cudaMemcpyHostToDevice, c->stream));
     BM_CUDA(cudaStreamSynchronize(c->stream));
     c->pattern_rmax = rmax;

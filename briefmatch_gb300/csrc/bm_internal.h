@@ -40,8 +40,15 @@ cudaError_t upsample_u8(const uint8_t* in, float* out, int sxi, int syi, int sxo
                         const float* lx, const int* ix, const float* ly, const int* iy, cudaStream_t st);
 cudaError_t u8_to_f32(const uint8_t* in, float* out, size_t n, cudaStream_t st);
 
+// Linear image offsets (o1, o2) of every BRIEF sample for one image width, padded
+// with zeros to a whole number of 32-bit words; passed by value as a kernel
+// parameter (4 KB) so that the sample loop reads them as constants.
+struct PatternOffsets {
+    int2 off[BM_PATCH_MAX / 4];
+};
+
 cudaError_t features(const float* up, uint32_t* F, int sx, int sy, int N, int nsp,
-                     const int4* pat, int rmax, cudaStream_t st);
+                     const int4* pat, int rmax, const PatternOffsets& po, cudaStream_t st);
 
 cudaError_t initialize(const uint32_t* F1, const uint32_t* F2, const uint32_t* flow_prev,
                        uint32_t* flow_out, uint16_t* cost, int sx, int sy, int nsp, int first,

@@ -147,37 +147,42 @@ __device__ __forceinline__ int hamming(const uint32_t (&a)[NSP], const uint32_t*
 
 template <int NSP>
 __global__ void __launch_bounds__(256) k_features(const float* __restrict__ I, uint32_t* __restrict__ F,
-                                                  int sx, int sy, int N, const int4* __restrict__ pat, int rmax)
+                                                  int sx, int sy, int N, const int4* __restrict__ pat, int rmax,
+                                                  const __grid_constant__ PatternOffsets po)
 {
     __shared__ int4 s_pat[BM_PATCH_MAX / 4];
-    __shared__ int2 s_off[BM_PATCH_MAX / 4];
-    const int tid = threadIdx.y * TX + threadIdx.x;
-    for (int s = tid; s < N; s += TX * TY) {
-        int4 q = pat[s];
-        s_pat[s] = q;
-        s_off[s] = make_int2(q.x + q.y * sx, q.z + q.w * sx);
-    }
-    __syncthreads();
     const int bx = blockIdx.x * TX, by = blockIdx.y * TY;
     const int x = bx + threadIdx.x, y = by + threadIdx.y;
-    if (x >= sx || y >= sy) return;
     const bool interior = (bx - rmax >= 0) && (bx + TX - 1 + rmax < sx) && (by - rmax >= 0) && (by + TY - 1 + rmax < sy);
-    const float* base = I + (size_t)y * sx + x;
     uint32_t word[NSP];
+    if (interior) {
+        // Every sample reads base + a linear offset held in the kernel's parameter
+        // space; the loop is fully unrolled so each offset is an immediate operand.
+        // Samples past N carry offset 0 and produce 0 bits.
+        const float* base = I + (size_t)y * sx + x;
 #pragma unroll
-    for (int wd = 0; wd < NSP; wd++) {
-        const int s0 = wd * 32;
-        const int cnt = min(32, N - s0);
-        uint32_t acc = 0;
-        if (interior) {
-#pragma unroll 8
-            for (int b = 0; b < cnt; b++) {
-                int2 o = s_off[s0 + b];
-                float i1 = __ldg(base + o.x);
-                float i2 = __ldg(base + o.y);
-                acc |= (i1 > i2 ? 1u : 0u) << b;
+        for (int wd = 0; wd < NSP; wd++) {
+            uint32_t acc = 0;
+#pragma unroll
+            for (int b = 0; b < 32; b++) {
+                const int2 o = po.off[wd * 32 + b];
+                const float i1 = __ldg(base + o.x);
+                const float i2 = __ldg(base + o.y);
+                if (i1 > i2) acc |= 1u << b;
             }
-        } else {
+            word[wd] = acc;
+        }
+    } else {
+        const int tid = threadIdx.y * TX + threadIdx.x;
+        for (int k = tid; k < N; k += TX * TY) s_pat[k] = pat[k];
+        __syncthreads();
+        if (x >= sx || y >= sy) return;
+        const float* base = I + (size_t)y * sx + x;
+#pragma unroll
+        for (int wd = 0; wd < NSP; wd++) {
+            const int s0 = wd * 32;
+            const int cnt = min(32, N - s0);
+            uint32_t acc = 0;
 #pragma unroll 4
             for (int b = 0; b < cnt; b++) {
                 int4 q = s_pat[s0 + b];
@@ -189,9 +194,10 @@ __global__ void __launch_bounds__(256) k_features(const float* __restrict__ I, u
                 float i2 = __ldg(base + ox2 + (long)oy2 * sx);
                 acc |= (i1 > i2 ? 1u : 0u) << b;
             }
+            word[wd] = acc;
         }
-        word[wd] = acc;
     }
+    if (x >= sx || y >= sy) return;
     store_desc<NSP>(F + ((size_t)y * sx + x) * NSP, word);
 }
 
@@ -251,67 +257,135 @@ __global__ void __launch_bounds__(256) k_initialize(const uint32_t* __restrict__
     flow_out[pix] = pack_flow(nx, ny);
 }
 
+// Descriptor loads for the own pixel: read once per level and never again, so
+// they are marked evict-first to leave L2 to the gathered descriptors.
 template <int NSP>
+__device__ __forceinline__ void load_desc_stream(uint32_t (&w)[NSP], const uint32_t* __restrict__ src)
+{
+    if constexpr (NSP >= 4) {
+#pragma unroll
+        for (int k = 0; k < NSP / 4; k++) {
+            uint4 v = __ldcs(reinterpret_cast<const uint4*>(src) + k);
+            w[4 * k] = v.x;
+            w[4 * k + 1] = v.y;
+            w[4 * k + 2] = v.z;
+            w[4 * k + 3] = v.w;
+        }
+    } else if constexpr (NSP == 2) {
+        uint2 v = __ldcs(reinterpret_cast<const uint2*>(src));
+        w[0] = v.x;
+        w[1] = v.y;
+    } else {
+        w[0] = __ldcs(src);
+    }
+}
+
+// Descriptor gather that is issued only when `pred` holds (the words stay zero
+// otherwise); written as predicated PTX loads so that several gathers of one
+// thread are in flight together instead of waiting behind each other's branches.
+template <int NSP>
+__device__ __forceinline__ void gather_desc_pred(uint32_t (&w)[NSP], const uint32_t* __restrict__ src, bool pred)
+{
+    const int pr = pred ? 1 : 0;
+#pragma unroll
+    for (int k = 0; k < NSP; k++) w[k] = 0;
+    if constexpr (NSP >= 4) {
+#pragma unroll
+        for (int k = 0; k < NSP / 4; k++)
+            asm("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t@p ld.global.nc.v4.u32 {%0, %1, %2, %3}, [%5];\n\t}"
+                : "+r"(w[4 * k]), "+r"(w[4 * k + 1]), "+r"(w[4 * k + 2]), "+r"(w[4 * k + 3])
+                : "r"(pr), "l"(src + 4 * k));
+    } else if constexpr (NSP == 2) {
+        asm("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %2, 0;\n\t@p ld.global.nc.v2.u32 {%0, %1}, [%3];\n\t}"
+            : "+r"(w[0]), "+r"(w[1])
+            : "r"(pr), "l"(src));
+    } else {
+        asm("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %1, 0;\n\t@p ld.global.nc.u32 %0, [%2];\n\t}"
+            : "+r"(w[0])
+            : "r"(pr), "l"(src));
+    }
+}
+
+// One jump-flood level.  All neighbour reads are issued together, then all
+// candidate descriptors are gathered together, and only then are the candidates
+// accepted in the reference's order (strictly lower cost wins).  Evaluating a
+// candidate that the reference would skip (equal to the current vector) or that
+// repeats an earlier one cannot change a decision, so those gathers are elided.
+// With RS the iteration's random-search candidate (briefmatch_cuda.cu:237-243) is
+// evaluated last; it reads nothing but this pixel's own state, so fusing it into
+// the last level gives the reference's result.
+template <int NSP, bool RS>
 __global__ void __launch_bounds__(256) k_jump_level(const uint32_t* __restrict__ F1, const uint32_t* __restrict__ F2,
                                                     const uint32_t* __restrict__ flow_in, uint32_t* __restrict__ flow_out,
                                                     uint16_t* __restrict__ cost, int sx, int sy,
                                                     int p, int pd, int doubleProp, RsArgs rs)
 {
+    constexpr int NC = RS ? 5 : 4;
     const int x = blockIdx.x * TX + threadIdx.x, y = blockIdx.y * TY + threadIdx.y;
     if (x >= sx || y >= sy) return;
     const long n = (long)sx * sy;
     const long pix = x + (long)y * sx;
-    const uint32_t own = flow_in[pix];
-    int cx = lo16(own), cy = hi16(own);
-    int h = cost[pix];
-    uint32_t f1[NSP];
-    load_desc<NSP>(f1, F1 + pix * NSP);
+    const uint32_t own = __ldg(flow_in + pix);
+    const int h0 = cost[pix];
 
-    uint32_t tried[4];
-    bool valid[4] = {false, false, false, false};
+    uint32_t cand[NC];
+    bool live[NC];
 #pragma unroll
     for (int c = 0; c < 4; c++) {
         const int d = (c < 2) ? -1 : 1;
         const int xy = c & 1;
-        if (d < 0 && !doubleProp) continue;
+        const bool active = d > 0 || doubleProp;
         const long doff = xy ? (long)pd * p * d : (long)sx * pd * p * d;
         const long q = pix + doff;
-        const uint32_t nb = (q >= 0 && q < n) ? flow_in[q] : 0u;
+        const uint32_t nb = (active && q >= 0 && q < n) ? __ldg(flow_in + q) : 0u;
         const int nx = min(max(lo16(nb), -x), sx - x - 1);
         const int ny = min(max(hi16(nb), -y), sy - y - 1);
-        if (nx == cx && ny == cy) continue;
-        const uint32_t key = pack_flow(nx, ny);
-        bool seen = false;
-#pragma unroll
-        for (int k = 0; k < c; k++)
-            if (valid[k] && tried[k] == key) seen = true;
-        if (seen) continue;
-        tried[c] = key;
-        valid[c] = true;
-        const int hc = hamming<NSP>(f1, F2 + (pix + nx + (long)ny * sx) * NSP);
-        if (hc < h) {
-            h = hc;
-            cx = nx;
-            cy = ny;
-        }
+        cand[c] = pack_flow(nx, ny);
+        live[c] = active;
     }
-
-    if (rs.enabled) {
+    if constexpr (RS) {
         float n1, n2;
         rs_normals(rs, (unsigned int)pix, n1, n2);
         const int nx = min(max((int)round(rs.dist * n1), -x), sx - x - 1);
         const int ny = min(max((int)round(rs.dist * n2), -y), sy - y - 1);
-        if (!(nx == cx && ny == cy)) {
-            const int hc = hamming<NSP>(f1, F2 + (pix + nx + (long)ny * sx) * NSP);
-            if (hc < h) {
-                h = hc;
-                cx = nx;
-                cy = ny;
-            }
-        }
+        cand[NC - 1] = pack_flow(nx, ny);
+        live[NC - 1] = true;
     }
-    flow_out[pix] = pack_flow(cx, cy);
-    cost[pix] = (uint16_t)h;
+#pragma unroll
+    for (int c = 0; c < NC; c++) {
+        bool dup = cand[c] == own;
+#pragma unroll
+        for (int k = 0; k < c; k++) dup = dup || (live[k] && cand[k] == cand[c]);
+        live[c] = live[c] && !dup;
+    }
+
+    uint32_t f1[NSP];
+    load_desc_stream<NSP>(f1, F1 + pix * NSP);
+    // predicated gathers, all in flight at once
+    uint32_t g[NC][NSP];
+#pragma unroll
+    for (int c = 0; c < NC; c++) {
+        const long t = pix + lo16(cand[c]) + (long)hi16(cand[c]) * sx;
+        gather_desc_pred<NSP>(g[c], F2 + t * NSP, live[c]);
+    }
+    int hc[NC];
+#pragma unroll
+    for (int c = 0; c < NC; c++) {
+        int acc = 0;
+#pragma unroll
+        for (int k = 0; k < NSP; k++) acc += __popc(f1[k] ^ g[c][k]);
+        hc[c] = live[c] ? acc : 0x7fffffff;
+    }
+    int h = h0;
+    uint32_t best = own;
+#pragma unroll
+    for (int c = 0; c < NC; c++)
+        if (hc[c] < h) {
+            h = hc[c];
+            best = cand[c];
+        }
+    flow_out[pix] = best;
+    if (h != h0) cost[pix] = (uint16_t)h;
 }
 
 template <int NSP>
@@ -456,21 +530,47 @@ __global__ void __launch_bounds__(256) k_median_pass(const float* __restrict__ i
 
 // ---------------------------------------------------------------------------
 // Cross-trilateral filter (briefmatch_cuda.cu:248-297).
-// The (2s+8) x (2s+32) neighbourhood of a 32x8 block is staged in shared memory
-// with clamp-to-edge addressing; the product of the three Gaussians is one exp2
-// of the summed exponents.
+// A block of 32x8 threads filters 32x32 output pixels; each thread owns four
+// vertically adjacent outputs, held as two pairs in packed f32x2 registers, so
+// every neighbourhood sample it reads from shared memory is used four times and
+// every arithmetic instruction serves two outputs.  The (2s+32)^2 neighbourhood
+// is staged in shared memory with clamp-to-edge addressing.
+// The three Gaussians are one exp2 of the summed exponents; the column factor
+// exp2(-cS*i^2) is applied once per column (the inner loop runs down a column).
+// Row factors outside the window are -inf, which gives weight 0.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_trilateral_smem(const float* __restrict__ U, const float* __restrict__ V,
-                                                         const float* __restrict__ Um, const float* __restrict__ Vm,
-                                                         const float* __restrict__ I, float* __restrict__ Uo,
-                                                         float* __restrict__ Vo, int sx, int sy, int s,
-                                                         float cE, float cI, float cS)
+typedef unsigned long long f2x;  // two packed floats (low = first)
+
+__device__ __forceinline__ f2x pk2(float a, float b) { f2x r; asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b)); return r; }
+__device__ __forceinline__ float lo2(f2x v) { float a, b; asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v)); return a; }
+__device__ __forceinline__ float hi2(f2x v) { float a, b; asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v)); return b; }
+__device__ __forceinline__ f2x add2(f2x a, f2x b) { f2x d; asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b)); return d; }
+__device__ __forceinline__ f2x sub2(f2x a, f2x b) { f2x d; asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b)); return d; }
+__device__ __forceinline__ f2x mul2(f2x a, f2x b) { f2x d; asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b)); return d; }
+__device__ __forceinline__ f2x fma2(f2x a, f2x b, f2x c)
 {
-    extern __shared__ float smem[];
-    const int TW = TX + 2 * s, TH = TY + 2 * s;
-    float2* suv = reinterpret_cast<float2*>(smem);
-    float* sI = smem + 2 * TW * TH;
-    const int x0 = blockIdx.x * TX - s, y0 = blockIdx.y * TY - s;
+    f2x d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ f2x ex2_2(f2x a) { return pk2(exp2f(lo2(a)), exp2f(hi2(a))); }
+
+constexpr int TRI_R = 4;             // outputs per thread (two f32x2 pairs)
+constexpr int TRI_BY = TY * TRI_R;   // output rows per block
+
+__global__ void __launch_bounds__(256) k_trilateral_x2(const float* __restrict__ U, const float* __restrict__ V,
+                                                       const float* __restrict__ Um, const float* __restrict__ Vm,
+                                                       const float* __restrict__ I, float* __restrict__ Uo,
+                                                       float* __restrict__ Vo, int sx, int sy, int s,
+                                                       float cE, float cI, float cS)
+{
+    extern __shared__ float4 smem4[];
+    const int TW = TX + 2 * s, TH = TRI_BY + 2 * s;
+    const int NR = 2 * s + TRI_R - 1;        // source rows a thread walks per column
+    float4* rowf = smem4;                    // [NR] exponents of the row factor for outputs r=0..3
+    float2* suv = reinterpret_cast<float2*>(smem4 + NR);
+    float* sI = reinterpret_cast<float*>(suv + TW * TH);
+    const int x0 = blockIdx.x * TX - s, y0 = blockIdx.y * TRI_BY - s;
     const int tid = threadIdx.y * TX + threadIdx.x;
     for (int k = tid; k < TW * TH; k += TX * TY) {
         const int r = k / TW, c = k - r * TW;
@@ -479,34 +579,83 @@ __global__ void __launch_bounds__(256) k_trilateral_smem(const float* __restrict
         suv[k] = make_float2(__ldg(U + g), __ldg(V + g));
         sI[k] = __ldg(I + g);
     }
+    for (int m = tid; m < NR; m += TX * TY) {
+        float t[TRI_R];
+#pragma unroll
+        for (int r = 0; r < TRI_R; r++) {
+            const int j = m - r - s;  // vertical offset of this source row for output r
+            t[r] = (j >= -s && j < s) ? -(float)(j * j) * cS : -__int_as_float(0x7f800000);
+        }
+        rowf[m] = make_float4(t[0], t[1], t[2], t[3]);
+    }
     __syncthreads();
-    const int x = blockIdx.x * TX + threadIdx.x, y = blockIdx.y * TY + threadIdx.y;
-    if (x >= sx || y >= sy) return;
-    const size_t o = (size_t)x + (size_t)y * sx;
-    const float um0 = Um[o], vm0 = Vm[o];
-    const float I0 = sI[(threadIdx.y + s) * TW + threadIdx.x + s];
-    float uf = 0.0f, vf = 0.0f, W = 0.0f;
+
+    const int x = blockIdx.x * TX + threadIdx.x;
+    const int yb = blockIdx.y * TRI_BY + threadIdx.y * TRI_R;
+    if (x >= sx || yb >= sy) return;
+    float umc[TRI_R], vmc[TRI_R], Ic[TRI_R];
+#pragma unroll
+    for (int r = 0; r < TRI_R; r++) {
+        const int yy = min(sy - 1, yb + r);
+        const size_t o = (size_t)x + (size_t)yy * sx;
+        umc[r] = __ldg(Um + o);
+        vmc[r] = __ldg(Vm + o);
+        Ic[r] = sI[(threadIdx.y * TRI_R + r + s) * TW + threadIdx.x + s];
+    }
+    const f2x umA = pk2(umc[0], umc[1]), umB = pk2(umc[2], umc[3]);
+    const f2x vmA = pk2(vmc[0], vmc[1]), vmB = pk2(vmc[2], vmc[3]);
+    const f2x IA = pk2(Ic[0], Ic[1]), IB = pk2(Ic[2], Ic[3]);
+    const f2x nE = pk2(-cE, -cE), nI = pk2(-cI, -cI);
+    f2x ufA = 0, ufB = 0, vfA = 0, vfB = 0, WA = 0, WB = 0;  // 0 bits = (0.0f, 0.0f)
+    const int row0 = threadIdx.y * TRI_R;
     for (int i = -s; i < s; i++) {
-        const float si = (float)(i * i) * cS;
-        const float2* col = suv + threadIdx.x + s + i + threadIdx.y * TW;
-        const float* colI = sI + threadIdx.x + s + i + threadIdx.y * TW;
-        for (int j = -s; j < s; j++) {
-            const int k = (j + s) * TW;
-            const float2 uv = col[k];
-            const float dI = colI[k] - I0;
-            const float du = uv.x - um0, dv = uv.y - vm0;
-            const float e = du * du + dv * dv;
-            const float sp = si + (float)(j * j) * cS;
-            const float arg = fmaf(e, -cE, fmaf(dI * dI, -cI, -sp));
-            const float w = exp2f(arg);
-            uf = fmaf(w, uv.x, uf);
-            vf = fmaf(w, uv.y, vf);
-            W += w;
+        const float2* col = suv + row0 * TW + threadIdx.x + s + i;
+        const float* colI = sI + row0 * TW + threadIdx.x + s + i;
+        f2x cuA = 0, cuB = 0, cvA = 0, cvB = 0, cwA = 0, cwB = 0;
+#pragma unroll 4
+        for (int m = 0; m < NR; m++) {
+            const float2 uv = col[m * TW];
+            const float i1 = colI[m * TW];
+            const float4 rf = rowf[m];
+            const f2x uu = pk2(uv.x, uv.x), vv = pk2(uv.y, uv.y), ii = pk2(i1, i1);
+            f2x du = sub2(uu, umA), dv = sub2(vv, vmA), dI = sub2(ii, IA);
+            f2x e = fma2(dv, dv, mul2(du, du));
+            f2x arg = fma2(mul2(dI, dI), nI, fma2(e, nE, pk2(rf.x, rf.y)));
+            f2x w = ex2_2(arg);
+            cuA = fma2(w, uu, cuA);
+            cvA = fma2(w, vv, cvA);
+            cwA = add2(cwA, w);
+            du = sub2(uu, umB);
+            dv = sub2(vv, vmB);
+            dI = sub2(ii, IB);
+            e = fma2(dv, dv, mul2(du, du));
+            arg = fma2(mul2(dI, dI), nI, fma2(e, nE, pk2(rf.z, rf.w)));
+            w = ex2_2(arg);
+            cuB = fma2(w, uu, cuB);
+            cvB = fma2(w, vv, cvB);
+            cwB = add2(cwB, w);
+        }
+        const float wi = exp2f(-(float)(i * i) * cS);
+        const f2x wi2 = pk2(wi, wi);
+        ufA = fma2(wi2, cuA, ufA);
+        ufB = fma2(wi2, cuB, ufB);
+        vfA = fma2(wi2, cvA, vfA);
+        vfB = fma2(wi2, cvB, vfB);
+        WA = fma2(wi2, cwA, WA);
+        WB = fma2(wi2, cwB, WB);
+    }
+    const float uf[TRI_R] = {lo2(ufA), hi2(ufA), lo2(ufB), hi2(ufB)};
+    const float vf[TRI_R] = {lo2(vfA), hi2(vfA), lo2(vfB), hi2(vfB)};
+    const float W[TRI_R] = {lo2(WA), hi2(WA), lo2(WB), hi2(WB)};
+#pragma unroll
+    for (int r = 0; r < TRI_R; r++) {
+        if (yb + r < sy) {
+            const size_t o = (size_t)x + (size_t)(yb + r) * sx;
+            const float Wc = fmaxf(1e-5f, W[r]);
+            Uo[o] = uf[r] / Wc;
+            Vo[o] = vf[r] / Wc;
         }
     }
-    const float Wc = fmaxf(1e-5f, W);
-    Uo[o] = uf / Wc;
-    Vo[o] = vf / Wc;
 }
 
 __global__ void __launch_bounds__(256) k_trilateral_global(const float* __restrict__ U, const float* __restrict__ V,
@@ -609,9 +758,9 @@ cudaError_t u8_to_f32(const uint8_t* in, float* out, size_t n, cudaStream_t st)
     }
 
 cudaError_t features(const float* up, uint32_t* F, int sx, int sy, int N, int nsp,
-                     const int4* pat, int rmax, cudaStream_t st)
+                     const int4* pat, int rmax, const PatternOffsets& po, cudaStream_t st)
 {
-    BM_DISPATCH_NSP(nsp, k_features<NSP><<<grid2d(sx, sy), dim3(TX, TY), 0, st>>>(up, F, sx, sy, N, pat, rmax));
+    BM_DISPATCH_NSP(nsp, k_features<NSP><<<grid2d(sx, sy), dim3(TX, TY), 0, st>>>(up, F, sx, sy, N, pat, rmax, po));
     return cudaGetLastError();
 }
 
@@ -627,7 +776,11 @@ cudaError_t jump_level(const uint32_t* F1, const uint32_t* F2, const uint32_t* f
                        uint32_t* flow_out, uint16_t* cost, int sx, int sy, int nsp,
                        int p, int pd, int doubleProp, const RsArgs& rs, cudaStream_t st)
 {
-    BM_DISPATCH_NSP(nsp, k_jump_level<NSP><<<grid2d(sx, sy), dim3(TX, TY), 0, st>>>(F1, F2, flow_in, flow_out, cost, sx, sy, p, pd, doubleProp, rs));
+    if (rs.enabled) {
+        BM_DISPATCH_NSP(nsp, k_jump_level<NSP, true><<<grid2d(sx, sy), dim3(TX, TY), 0, st>>>(F1, F2, flow_in, flow_out, cost, sx, sy, p, pd, doubleProp, rs));
+    } else {
+        BM_DISPATCH_NSP(nsp, k_jump_level<NSP, false><<<grid2d(sx, sy), dim3(TX, TY), 0, st>>>(F1, F2, flow_in, flow_out, cost, sx, sy, p, pd, doubleProp, rs));
+    }
     return cudaGetLastError();
 }
 
@@ -691,11 +844,13 @@ cudaError_t trilateral(const float* U, const float* V, const float* Um, const fl
     const float cE = LOG2E / (2.0f * sigmaEPE2);
     const float cI = LOG2E / (2.0f * sigmaI2 * 255.0f * 255.0f);
     const float cS = LOG2E / (2.0f * sigmaS2);
-    const size_t smem = (size_t)(TX + 2 * s) * (TY + 2 * s) * 3 * sizeof(float);
-    if (smem <= 200 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(k_trilateral_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const size_t smem = (size_t)(2 * s + TRI_R - 1) * sizeof(float4) +
+                        (size_t)(TX + 2 * s) * (TRI_BY + 2 * s) * 3 * sizeof(float);
+    if (smem <= 220 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(k_trilateral_x2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        k_trilateral_smem<<<grid2d(sx, sy), dim3(TX, TY), smem, st>>>(U, V, Um, Vm, I, Uo, Vo, sx, sy, s, cE, cI, cS);
+        dim3 g((sx + TX - 1) / TX, (sy + TRI_BY - 1) / TRI_BY);
+        k_trilateral_x2<<<g, dim3(TX, TY), smem, st>>>(U, V, Um, Vm, I, Uo, Vo, sx, sy, s, cE, cI, cS);
     } else {
         k_trilateral_global<<<grid2d(sx, sy), dim3(TX, TY), 0, st>>>(U, V, Um, Vm, I, Uo, Vo, sx, sy, s, cE, cI, cS);
     }
