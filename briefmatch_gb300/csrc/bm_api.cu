@@ -85,6 +85,7 @@ struct bm_ctx {
     float dist = 0;          // random-search radius, briefmatch.cpp:271
     int tri_s = 0;           // trilateral half window, briefmatch_cuda.cu:266
     uint64_t rs_calls = 0;   // random-search calls made so far
+    int pass_rev = 0;        // visiting order of the next full-frame pass (alternates)
     bool first_match = true; // BriefMatch::m_firstFrame
     bool primed = false;
     uint64_t launches = 0;
@@ -194,6 +195,13 @@ bm_status check_ctx(const bm_ctx* c)
     return BM_OK;
 }
 
+int next_order(bm_ctx* c)
+{
+    const int r = c->pass_rev;
+    c->pass_rev ^= 1;
+    return r;
+}
+
 bmk::RsArgs rs_args(const bm_ctx* c, bool enabled)
 {
     bmk::RsArgs rs;
@@ -209,7 +217,7 @@ bm_status features_into(bm_ctx* c, const float* d_up, uint32_t* F)
 {
     const bm_params& p = c->prm;
     BM_LAUNCH(c, "features", bmk::features(d_up, F, (int)p.sx, (int)p.sy, (int)p.N, (int)c->nsp, c->d_pattern, c->pattern_rmax,
-                               c->pattern_off, c->stream));
+                               c->pattern_off, next_order(c), c->stream));
     return BM_OK;
 }
 
@@ -226,7 +234,7 @@ bm_status propagate_pass(bm_ctx* c, int pd, bool fuse_rs)
         bmk::RsArgs rs = rs_args(c, fuse_rs && last);
         BM_LAUNCH(c, rs.enabled ? "jump_level_rs" : "jump_level", bmk::jump_level(c->feat1_ptr(), c->feat2_ptr(), c->d_flow[c->flow_cur], c->d_flow[c->flow_cur ^ 1],
                                      c->d_cost, (int)p.sx, (int)p.sy, (int)c->nsp, step, pd, p.doubleProp ? 1 : 0, rs,
-                                     c->stream));
+                                     next_order(c), c->stream));
         c->flow_cur ^= 1;
     }
     if (fuse_rs) {
@@ -247,7 +255,7 @@ bm_status match_impl(bm_ctx* c, const float* d_im2)
     if (st != BM_OK) return st;
     const int first = (c->first_match || !p.tInit) ? 1 : 0;
     BM_LAUNCH(c, "initialize", bmk::initialize(c->feat1_ptr(), c->feat2_ptr(), c->d_flow[c->flow_cur], c->d_flow[c->flow_cur ^ 1],
-                                 c->d_cost, (int)p.sx, (int)p.sy, (int)c->nsp, first, c->stream));
+                                 c->d_cost, (int)p.sx, (int)p.sy, (int)c->nsp, first, next_order(c), c->stream));
     c->flow_cur ^= 1;
     int pd = -1;
     for (uint32_t it = 0; it < p.iterations; it++) {
@@ -571,7 +579,7 @@ bm_status bm_initialize(bm_ctx* c, int first)
     if (check_ctx(c)) return BM_ERR_INVALID;
     const bm_params& p = c->prm;
     BM_LAUNCH(c, "initialize", bmk::initialize(c->feat1_ptr(), c->feat2_ptr(), c->d_flow[c->flow_cur], c->d_flow[c->flow_cur ^ 1],
-                                 c->d_cost, (int)p.sx, (int)p.sy, (int)c->nsp, first ? 1 : 0, c->stream));
+                                 c->d_cost, (int)p.sx, (int)p.sy, (int)c->nsp, first ? 1 : 0, next_order(c), c->stream));
     c->flow_cur ^= 1;
     return BM_OK;
 }

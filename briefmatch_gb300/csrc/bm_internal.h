@@ -48,15 +48,15 @@ struct PatternOffsets {
 };
 
 cudaError_t features(const float* up, uint32_t* F, int sx, int sy, int N, int nsp,
-                     const int4* pat, int rmax, const PatternOffsets& po, cudaStream_t st);
+                     const int4* pat, int rmax, const PatternOffsets& po, int rev, cudaStream_t st);
 
 cudaError_t initialize(const uint32_t* F1, const uint32_t* F2, const uint32_t* flow_prev,
-                       uint32_t* flow_out, uint16_t* cost, int sx, int sy, int nsp, int first,
+                       uint32_t* flow_out, uint16_t* cost, int sx, int sy, int nsp, int first, int rev,
                        cudaStream_t st);
 
 cudaError_t jump_level(const uint32_t* F1, const uint32_t* F2, const uint32_t* flow_in,
                        uint32_t* flow_out, uint16_t* cost, int sx, int sy, int nsp,
-                       int p, int pd, int doubleProp, const RsArgs& rs, cudaStream_t st);
+                       int p, int pd, int doubleProp, const RsArgs& rs, int rev, cudaStream_t st);
 
 cudaError_t random_search(const uint32_t* F1, const uint32_t* F2, uint32_t* flow, uint16_t* cost,
                           int sx, int sy, int nsp, const RsArgs& rs, cudaStream_t st);

@@ -30,6 +30,19 @@ __device__ __forceinline__ int hi16(uint32_t w) { return (int)(int16_t)(w >> 16)
 
 inline dim3 grid2d(int w, int h) { return dim3((w + TX - 1) / TX, (h + TY - 1) / TY); }
 
+// Tile visited by this block.  Full-frame passes alternate their visiting order
+// (raster, then reverse raster): a pass that follows one in the other direction
+// starts on the tiles its predecessor touched last, which are still in L2.
+__device__ __forceinline__ int2 block_tile(int rev)
+{
+    int bx = blockIdx.x, by = blockIdx.y;
+    if (rev) {
+        bx = gridDim.x - 1 - bx;
+        by = gridDim.y - 1 - by;
+    }
+    return make_int2(bx * TX, by * TY);
+}
+
 // ---------------------------------------------------------------------------
 // Lanczos-3 up-sampling (util_cuda.cu:126-158).
 // The weights depend on x only (resp. y only), so they are tabulated once per
@@ -148,10 +161,11 @@ __device__ __forceinline__ int hamming(const uint32_t (&a)[NSP], const uint32_t*
 template <int NSP>
 __global__ void __launch_bounds__(256) k_features(const float* __restrict__ I, uint32_t* __restrict__ F,
                                                   int sx, int sy, int N, const int4* __restrict__ pat, int rmax,
-                                                  const __grid_constant__ PatternOffsets po)
+                                                  const __grid_constant__ PatternOffsets po, int rev)
 {
     __shared__ int4 s_pat[BM_PATCH_MAX / 4];
-    const int bx = blockIdx.x * TX, by = blockIdx.y * TY;
+    const int2 t0 = block_tile(rev);
+    const int bx = t0.x, by = t0.y;
     const int x = bx + threadIdx.x, y = by + threadIdx.y;
     const bool interior = (bx - rmax >= 0) && (bx + TX - 1 + rmax < sx) && (by - rmax >= 0) && (by + TY - 1 + rmax < sy);
     uint32_t word[NSP];
@@ -237,9 +251,10 @@ __device__ __forceinline__ void rs_normals(const RsArgs& rs, unsigned int id, fl
 template <int NSP>
 __global__ void __launch_bounds__(256) k_initialize(const uint32_t* __restrict__ F1, const uint32_t* __restrict__ F2,
                                                     const uint32_t* __restrict__ flow_prev, uint32_t* __restrict__ flow_out,
-                                                    uint16_t* __restrict__ cost, int sx, int sy, int first)
+                                                    uint16_t* __restrict__ cost, int sx, int sy, int first, int rev)
 {
-    const int x = blockIdx.x * TX + threadIdx.x, y = blockIdx.y * TY + threadIdx.y;
+    const int2 t0 = block_tile(rev);
+    const int x = t0.x + threadIdx.x, y = t0.y + threadIdx.y;
     if (x >= sx || y >= sy) return;
     const long n = (long)sx * sy;
     const long pix = x + (long)y * sx;
@@ -318,10 +333,11 @@ template <int NSP, bool RS>
 __global__ void __launch_bounds__(256) k_jump_level(const uint32_t* __restrict__ F1, const uint32_t* __restrict__ F2,
                                                     const uint32_t* __restrict__ flow_in, uint32_t* __restrict__ flow_out,
                                                     uint16_t* __restrict__ cost, int sx, int sy,
-                                                    int p, int pd, int doubleProp, RsArgs rs)
+                                                    int p, int pd, int doubleProp, RsArgs rs, int rev)
 {
     constexpr int NC = RS ? 5 : 4;
-    const int x = blockIdx.x * TX + threadIdx.x, y = blockIdx.y * TY + threadIdx.y;
+    const int2 t0 = block_tile(rev);
+    const int x = t0.x + threadIdx.x, y = t0.y + threadIdx.y;
     if (x >= sx || y >= sy) return;
     const long n = (long)sx * sy;
     const long pix = x + (long)y * sx;
@@ -758,28 +774,28 @@ cudaError_t u8_to_f32(const uint8_t* in, float* out, size_t n, cudaStream_t st)
     }
 
 cudaError_t features(const float* up, uint32_t* F, int sx, int sy, int N, int nsp,
-                     const int4* pat, int rmax, const PatternOffsets& po, cudaStream_t st)
+                     const int4* pat, int rmax, const PatternOffsets& po, int rev, cudaStream_t st)
 {
-    BM_DISPATCH_NSP(nsp, k_features<NSP><<<grid2d(sx, sy), dim3(TX, TY), 0, st>>>(up, F, sx, sy, N, pat, rmax, po));
+    BM_DISPATCH_NSP(nsp, k_features<NSP><<<grid2d(sx, sy), dim3(TX, TY), 0, st>>>(up, F, sx, sy, N, pat, rmax, po, rev));
     return cudaGetLastError();
 }
 
 cudaError_t initialize(const uint32_t* F1, const uint32_t* F2, const uint32_t* flow_prev,
-                       uint32_t* flow_out, uint16_t* cost, int sx, int sy, int nsp, int first,
+                       uint32_t* flow_out, uint16_t* cost, int sx, int sy, int nsp, int first, int rev,
                        cudaStream_t st)
 {
-    BM_DISPATCH_NSP(nsp, k_initialize<NSP><<<grid2d(sx, sy), dim3(TX, TY), 0, st>>>(F1, F2, flow_prev, flow_out, cost, sx, sy, first));
+    BM_DISPATCH_NSP(nsp, k_initialize<NSP><<<grid2d(sx, sy), dim3(TX, TY), 0, st>>>(F1, F2, flow_prev, flow_out, cost, sx, sy, first, rev));
     return cudaGetLastError();
 }
 
 cudaError_t jump_level(const uint32_t* F1, const uint32_t* F2, const uint32_t* flow_in,
                        uint32_t* flow_out, uint16_t* cost, int sx, int sy, int nsp,
-                       int p, int pd, int doubleProp, const RsArgs& rs, cudaStream_t st)
+                       int p, int pd, int doubleProp, const RsArgs& rs, int rev, cudaStream_t st)
 {
     if (rs.enabled) {
-        BM_DISPATCH_NSP(nsp, k_jump_level<NSP, true><<<grid2d(sx, sy), dim3(TX, TY), 0, st>>>(F1, F2, flow_in, flow_out, cost, sx, sy, p, pd, doubleProp, rs));
+        BM_DISPATCH_NSP(nsp, k_jump_level<NSP, true><<<grid2d(sx, sy), dim3(TX, TY), 0, st>>>(F1, F2, flow_in, flow_out, cost, sx, sy, p, pd, doubleProp, rs, rev));
     } else {
-        BM_DISPATCH_NSP(nsp, k_jump_level<NSP, false><<<grid2d(sx, sy), dim3(TX, TY), 0, st>>>(F1, F2, flow_in, flow_out, cost, sx, sy, p, pd, doubleProp, rs));
+        BM_DISPATCH_NSP(nsp, k_jump_level<NSP, false><<<grid2d(sx, sy), dim3(TX, TY), 0, st>>>(F1, F2, flow_in, flow_out, cost, sx, sy, p, pd, doubleProp, rs, rev));
     }
     return cudaGetLastError();
 }
