@@ -546,7 +546,7 @@ __global__ void __launch_bounds__(256) k_median_pass(const float* __restrict__ i
 
 // ---------------------------------------------------------------------------
 // Cross-trilateral filter (briefmatch_cuda.cu:248-297).
-// A block of 32x8 threads filters 32x32 output pixels; each thread owns four
+// A block of 32x4 threads filters 32x16 output pixels; each thread owns four
 // vertically adjacent outputs, held as two pairs in packed f32x2 registers, so
 // every neighbourhood sample it reads from shared memory is used four times and
 // every arithmetic instruction serves two outputs.  The (2s+32)^2 neighbourhood
@@ -571,10 +571,11 @@ __device__ __forceinline__ f2x fma2(f2x a, f2x b, f2x c)
 }
 __device__ __forceinline__ f2x ex2_2(f2x a) { return pk2(exp2f(lo2(a)), exp2f(hi2(a))); }
 
-constexpr int TRI_R = 4;             // outputs per thread (two f32x2 pairs)
-constexpr int TRI_BY = TY * TRI_R;   // output rows per block
+constexpr int TRI_R = 4;              // outputs per thread (two f32x2 pairs)
+constexpr int TRI_TY = 4;             // thread rows per block
+constexpr int TRI_BY = TRI_TY * TRI_R;  // output rows per block (32x16 outputs: ~3 blocks per SM at s=24)
 
-__global__ void __launch_bounds__(256) k_trilateral_x2(const float* __restrict__ U, const float* __restrict__ V,
+__global__ void __launch_bounds__(TX * TRI_TY) k_trilateral_x2(const float* __restrict__ U, const float* __restrict__ V,
                                                        const float* __restrict__ Um, const float* __restrict__ Vm,
                                                        const float* __restrict__ I, float* __restrict__ Uo,
                                                        float* __restrict__ Vo, int sx, int sy, int s,
@@ -588,14 +589,14 @@ __global__ void __launch_bounds__(256) k_trilateral_x2(const float* __restrict__
     float* sI = reinterpret_cast<float*>(suv + TW * TH);
     const int x0 = blockIdx.x * TX - s, y0 = blockIdx.y * TRI_BY - s;
     const int tid = threadIdx.y * TX + threadIdx.x;
-    for (int k = tid; k < TW * TH; k += TX * TY) {
+    for (int k = tid; k < TW * TH; k += TX * TRI_TY) {
         const int r = k / TW, c = k - r * TW;
         const int gx = min(sx - 1, max(0, x0 + c)), gy = min(sy - 1, max(0, y0 + r));
         const size_t g = (size_t)gx + (size_t)gy * sx;
         suv[k] = make_float2(__ldg(U + g), __ldg(V + g));
         sI[k] = __ldg(I + g);
     }
-    for (int m = tid; m < NR; m += TX * TY) {
+    for (int m = tid; m < NR; m += TX * TRI_TY) {
         float t[TRI_R];
 #pragma unroll
         for (int r = 0; r < TRI_R; r++) {
@@ -866,7 +867,7 @@ cudaError_t trilateral(const float* U, const float* V, const float* Um, const fl
         cudaError_t e = cudaFuncSetAttribute(k_trilateral_x2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         dim3 g((sx + TX - 1) / TX, (sy + TRI_BY - 1) / TRI_BY);
-        k_trilateral_x2<<<g, dim3(TX, TY), smem, st>>>(U, V, Um, Vm, I, Uo, Vo, sx, sy, s, cE, cI, cS);
+        k_trilateral_x2<<<g, dim3(TX, TRI_TY), smem, st>>>(U, V, Um, Vm, I, Uo, Vo, sx, sy, s, cE, cI, cS);
     } else {
         k_trilateral_global<<<grid2d(sx, sy), dim3(TX, TY), 0, st>>>(U, V, Um, Vm, I, Uo, Vo, sx, sy, s, cE, cI, cS);
     }
