@@ -103,6 +103,9 @@ def _declare(lib):
         "bm_profile_enable": (c.c_int, [c.c_void_p, c.c_int]),
         "bm_profile_reset": (c.c_int, [c.c_void_p]),
         "bm_profile_read": (c.c_int, [c.c_void_p, c.c_void_p, c.c_uint32, P(c.c_uint32)]),
+        "bm_refine_noalloc": (c.c_int, [c.c_void_p, c.c_void_p, c.c_void_p, c.c_void_p, c.c_void_p, c.c_uint32,
+                                        c.c_uint32, c.c_uint32, c.c_float, c.c_float, c.c_float, c.c_void_p]),
+        "bm_refine_noalloc_max_pixels": (c.c_uint64, []),
         "bm_last_error": (c.c_char_p, []),
         "bm_version": (c.c_char_p, []),
     }
@@ -367,6 +370,14 @@ class FlowEngine(BriefMatch):
         v = np.empty((p.sy_in, p.sx_in), np.float32)
         self.frame(f.ctypes.data, False, u.ctypes.data, v.ctypes.data, out_on_device=False)
         return u, v
+
+
+def refine_noalloc(d_u, d_v, d_guide, d_uo, d_vo, width, height, fsize, sEPE, sI, sS, stream=0):
+    """Median + cross-trilateral refinement on caller-owned device buffers without
+    any device allocation (fixed scratch in the library; see bm_refine_noalloc)."""
+    check(lib().bm_refine_noalloc(ctypes.c_void_p(d_u), ctypes.c_void_p(d_v), ctypes.c_void_p(d_guide),
+                                  ctypes.c_void_p(d_uo), ctypes.c_void_p(d_vo), width, height, fsize, sEPE, sI, sS,
+                                  ctypes.c_void_p(stream)))
 
 
 def version():

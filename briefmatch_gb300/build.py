@@ -40,6 +40,7 @@ NVCC_COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ff
 ENGINE_UNITS = [
     ("bm_kernels.cu", ["-use_fast_math", "-Xptxas", "-v"]),
     ("bm_api.cu", []),
+    ("bm_noalloc.cu", []),
     ("bm_params.cpp", []),
 ]
 

@@ -51,6 +51,8 @@ bm_status fail(bm_status st, const char* fmt, ...)
 
 }  // namespace
 
+void bmk::set_error_text(const char* msg) { g_last_error = msg ? msg : ""; }
+
 struct bm_ctx {
     bm_params prm;
     uint32_t nsp = 1;

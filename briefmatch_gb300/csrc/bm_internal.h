@@ -9,6 +9,9 @@
 
 namespace bmk {
 
+// Sets the text bm_last_error() returns on this thread.
+void set_error_text(const char* msg);
+
 // Random-search stream position for one launch (briefmatch_cuda.cu:237-241).
 struct RsArgs {
     int enabled;                 // fuse a random-search candidate into the launch

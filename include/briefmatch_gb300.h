@@ -192,6 +192,29 @@ bm_status bm_nn_indices(bm_ctx* ctx, uint32_t* h_x, uint32_t* h_y);
 bm_status bm_rng_position(bm_ctx* ctx, uint64_t* calls);
 bm_status bm_set_rng_position(bm_ctx* ctx, uint64_t calls);
 
+/* ---- refinement without allocation ------------------------------------------------ */
+
+/* No counterpart in the reference.  The refinement of bm_process (median filter
+ * then cross-trilateral filter) on caller-owned device buffers, for callers that
+ * cannot allocate device memory while running (pipelines that allocate only at
+ * start-up, plugin hosts that own the memory budget, threads that must not take
+ * the device synchronisation of cudaMalloc/cudaFree).  It calls no allocator:
+ * its intermediate planes live in a fixed 32 MiB array compiled into the library,
+ * which every GPU that loads the library holds until the process exits, so it
+ * accepts at most bm_refine_noalloc_max_pixels() (2,097,152) input pixels and
+ * returns BM_ERR_LIMIT above that.  d_u, d_v: input field, d_guide: previous
+ * input frame (0..255), d_uo, d_vo: output field; all width*height floats.
+ * stream is a cudaStream_t (NULL = legacy default stream).  The first call on a
+ * device looks up the array's device address with that device current; make that
+ * first call before any stream capture.  All calls share the one array: calls whose
+ * work overlaps on the GPU (different streams, or host threads without ordering)
+ * race on it; the array needs no clearing between calls, since every element is
+ * written before it is read. */
+bm_status bm_refine_noalloc(const float* d_u, const float* d_v, const float* d_guide, float* d_uo, float* d_vo,
+                            uint32_t width, uint32_t height, uint32_t fsize, float sEPE, float sI, float sS,
+                            void* stream);
+uint64_t bm_refine_noalloc_max_pixels(void);
+
 /* ---- one frame (OFPipeline::processFrame, of_pipeline.cpp:241-333) --------------- */
 
 /* Feed the next 8-bit frame (sx_in*sy_in bytes, row-major).  frame_on_device says
