@@ -168,12 +168,12 @@ def algorithmic_bytes(kernel, prm):
     n = prm.sx * prm.sy
     ni = prm.sx_in * prm.sy_in
     ns = (prm.N + 31) // 32
-    cands = 4 if prm.doubleProp else 2
     table = {
-        # per pixel: the candidates' descriptors gathered, the field read and written
-        # (4 B) and the cost read and written (2 B each)
-        "jump_level": n * (cands * ns * 4 + 2 * 4 + 2 * 2),
-        "jump_level_rs": n * ((cands + 1) * ns * 4 + 2 * 4 + 2 * 2),
+        # per pixel and level, the working set each level moves at least once: own
+        # descriptor, the gathered frame's descriptor footprint, field read and
+        # written (4 B each), cost read and written (2 B each); 44 B at N=128
+        "jump_level": n * (2 * ns * 4 + 2 * 4 + 2 * 2),
+        "jump_level_rs": n * (2 * ns * 4 + 2 * 4 + 2 * 2),
         # up-sampled image read once, descriptors written once
         "features": n * (4 + ns * 4),
         "initialize": n * (2 * ns * 4 + 4 + 2),

@@ -4,6 +4,7 @@ Everything is compiled in-tree with nvcc/gcc directly (no cmake), translation
 units in parallel:
 
   briefmatch_gb300/_lib/libbriefmatch_gb300.so   engine (CUDA kernels + C ABI)
+  briefmatch_gb300/_lib/briefmatch                command line (C++ BriefMatch/OFPipeline)
   oracle/_build/libbmoracle.so                    CPU restatement (test infrastructure)
   oracle/_build/librefshim.so                     loader for the reference kernel build
   oracle/_ref/*.cubin                             reference kernels compiled from their
@@ -94,6 +95,40 @@ def build_engine(force=False, verbose=False):
     return LIB
 
 
+CXX_DIR = os.path.join(CSRC, "cxx")
+CXX_UNITS = ["briefmatch.cpp", "of_pipeline.cpp", "flow_io.cpp", "main.cpp"]
+CLI = os.path.join(LIBDIR, "briefmatch")
+
+
+def _have_zlib():
+    probe = os.path.join(BUILD, "zprobe.c")
+    with open(probe, "w") as f:
+        f.write("#include <zlib.h>\nint main(void){return (int)zlibVersion()[0] == 0;}\n")
+    p = subprocess.run(["gcc", probe, "-lz", "-o", os.path.join(BUILD, "zprobe")], stdout=subprocess.PIPE,
+                       stderr=subprocess.STDOUT)
+    return p.returncode == 0
+
+
+def build_cli(force=False):
+    """The briefmatch command line: the reference's BriefMatch/OFPipeline API (C++)
+    over the engine library, linked with rpath $ORIGIN.  PNG I/O needs zlib; without
+    it the CLI reads PGM/PPM and writes .flo/.bin only."""
+    os.makedirs(BUILD, exist_ok=True)
+    zlib = _have_zlib()
+    srcs = [os.path.join(CXX_DIR, u) for u in CXX_UNITS]
+    hdrs = [os.path.join(CXX_DIR, f) for f in os.listdir(CXX_DIR) if f.endswith(".h")] + _headers()
+    if not (force or _newer(CLI, srcs + hdrs + [LIB])):
+        return CLI
+    cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-I" + os.path.join(ROOT, "include"), "-I" + CXX_DIR]
+    if zlib:
+        cmd.append("-DBM_HAVE_ZLIB")
+    cmd += srcs + ["-o", CLI, "-L" + LIBDIR, "-lbriefmatch_gb300", "-Wl,-rpath,$ORIGIN"]
+    if zlib:
+        cmd.append("-lz")
+    _run(cmd)
+    return CLI
+
+
 def build_oracle(force=False):
     os.makedirs(ORACLE_BUILD, exist_ok=True)
     src = os.path.join(ORACLE_DIR, "bm_oracle.c")
@@ -138,7 +173,9 @@ def build_all(force=False, verbose=False):
         f1 = ex.submit(build_engine, force, verbose)
         f2 = ex.submit(build_oracle, force)
         f3 = ex.submit(build_reference, "/root/reference", force)
-        return f1.result(), f2.result(), f3.result()
+        lib = f1.result()
+        cli = build_cli(force)
+        return lib, cli, f2.result(), f3.result()
 
 
 if __name__ == "__main__":
