@@ -106,6 +106,24 @@ def _declare(lib):
         "bm_refine_noalloc": (c.c_int, [c.c_void_p, c.c_void_p, c.c_void_p, c.c_void_p, c.c_void_p, c.c_uint32,
                                         c.c_uint32, c.c_uint32, c.c_float, c.c_float, c.c_float, c.c_void_p]),
         "bm_refine_noalloc_max_pixels": (c.c_uint64, []),
+        "bm_batch_create": (c.c_int, [c.c_void_p, c.c_uint32, P(c.c_void_p)]),
+        "bm_batch_destroy": (c.c_int, [c.c_void_p]),
+        "bm_batch_count": (c.c_uint32, [c.c_void_p]),
+        "bm_batch_set_stream": (c.c_int, [c.c_void_p, c.c_void_p]),
+        "bm_batch_set_pattern": (c.c_int, [c.c_void_p, c.c_uint32, c.c_void_p, c.c_uint32]),
+        "bm_batch_frames_bytes": (c.c_size_t, [c.c_void_p]),
+        "bm_batch_flows_bytes": (c.c_size_t, [c.c_void_p]),
+        "bm_batch_frame_ptr": (c.c_int, [c.c_void_p, c.c_uint32, c.c_uint32, P(c.c_void_p)]),
+        "bm_batch_load_frames": (c.c_int, [c.c_void_p, c.c_void_p, c.c_size_t, c.c_int]),
+        "bm_batch_read_flows": (c.c_int, [c.c_void_p, c.c_void_p, c.c_size_t, c.c_int]),
+        "bm_batch_flow_ptr": (c.c_int, [c.c_void_p, c.c_uint32, P(c.c_void_p), P(c.c_void_p)]),
+        "bm_batch_set_schedule": (c.c_int, [c.c_void_p, c.c_void_p]),
+        "bm_batch_get_schedule": (c.c_int, [c.c_void_p, c.c_void_p]),
+        "bm_batch_run": (c.c_int, [c.c_void_p]),
+        "bm_batch_synchronize": (c.c_int, [c.c_void_p]),
+        "bm_batch_launch_count": (c.c_uint64, [c.c_void_p]),
+        "bm_batch_autotune": (c.c_int, [c.c_void_p, c.c_char_p, c.c_int, c.c_char_p, c.c_size_t]),
+        "bm_selftest_barrier": (c.c_int, [c.c_uint32, c.c_uint32, c.c_uint64, P(c.c_int)]),
         "bm_last_error": (c.c_char_p, []),
         "bm_version": (c.c_char_p, []),
     }
@@ -370,6 +388,112 @@ class FlowEngine(BriefMatch):
         v = np.empty((p.sy_in, p.sx_in), np.float32)
         self.frame(f.ctypes.data, False, u.ctypes.data, v.ctypes.data, out_on_device=False)
         return u, v
+
+
+class bm_batch_schedule(ctypes.Structure):
+    _fields_ = [("persistent", ctypes.c_uint32), ("blocks_per_sm", ctypes.c_uint32), ("snake", ctypes.c_uint32),
+                ("use_graph", ctypes.c_uint32), ("spin_limit", ctypes.c_uint64)]
+
+
+class Batch:
+    """Many frame pairs of uneven size computed together (bm_batch_* in the C ABI).
+
+    ``params`` is one BMParams per pair (all with the same N, iterations, jfMax,
+    doubleProp, filter and random stream).  Pair i's result equals what a fresh
+    FlowEngine computes for its two frames."""
+
+    def __init__(self, params):
+        arr = (bm_params * len(params))(*[p.struct() for p in params])
+        self.params = list(params)
+        self._b = ctypes.c_void_p(None)
+        check(lib().bm_batch_create(arr, len(params), ctypes.byref(self._b)))
+        self.frames_bytes = lib().bm_batch_frames_bytes(self._b)
+        self.flows_bytes = lib().bm_batch_flows_bytes(self._b)
+
+    def close(self):
+        if self._b:
+            lib().bm_batch_destroy(self._b)
+            self._b = ctypes.c_void_p(None)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_ptr):
+        check(lib().bm_batch_set_stream(self._b, ctypes.c_void_p(stream_ptr)))
+
+    def set_pattern(self, pair, pattern):
+        pat = np.ascontiguousarray(pattern, np.float32)
+        check(lib().bm_batch_set_pattern(self._b, pair, pat.ctypes.data, pat.size))
+
+    def pack_frames(self, pairs_of_frames):
+        """Host packing of [(frame0, frame1), ...] in the batch's frame layout."""
+        parts = []
+        for (f0, f1), p in zip(pairs_of_frames, self.params):
+            for f in (f0, f1):
+                f = np.ascontiguousarray(f, np.uint8)
+                assert f.shape == (p.sy_in, p.sx_in)
+                parts.append(f.ravel())
+        out = np.concatenate(parts)
+        assert out.nbytes == self.frames_bytes
+        return out
+
+    def load_frames(self, packed, on_device=False):
+        ptr = packed if isinstance(packed, int) else packed.ctypes.data
+        check(lib().bm_batch_load_frames(self._b, ctypes.c_void_p(ptr), self.frames_bytes, int(bool(on_device))))
+
+    def frame_ptr(self, pair, which):
+        p = ctypes.c_void_p(None)
+        check(lib().bm_batch_frame_ptr(self._b, pair, which, ctypes.byref(p)))
+        return p.value
+
+    def run(self):
+        check(lib().bm_batch_run(self._b))
+
+    def synchronize(self):
+        check(lib().bm_batch_synchronize(self._b))
+
+    def read_flows(self):
+        out = np.empty(self.flows_bytes // 4, np.float32)
+        check(lib().bm_batch_read_flows(self._b, out.ctypes.data, self.flows_bytes, 0))
+        res, k = [], 0
+        for p in self.params:
+            n = p.sx_in * p.sy_in
+            res.append((out[k:k + n].reshape(p.sy_in, p.sx_in), out[k + n:k + 2 * n].reshape(p.sy_in, p.sx_in)))
+            k += 2 * n
+        return res
+
+    def read_flows_into(self, ptr, on_device):
+        check(lib().bm_batch_read_flows(self._b, ctypes.c_void_p(ptr), self.flows_bytes, int(bool(on_device))))
+
+    def schedule(self):
+        s = bm_batch_schedule()
+        check(lib().bm_batch_get_schedule(self._b, ctypes.byref(s)))
+        return {k: getattr(s, k) for k, _ in s._fields_}
+
+    def set_schedule(self, **kw):
+        s = bm_batch_schedule()
+        check(lib().bm_batch_get_schedule(self._b, ctypes.byref(s)))
+        for k, v in kw.items():
+            setattr(s, k, v)
+        check(lib().bm_batch_set_schedule(self._b, ctypes.byref(s)))
+
+    def autotune(self, cache_path=None, reps=3):
+        buf = ctypes.create_string_buffer(2048)
+        check(lib().bm_batch_autotune(self._b, cache_path.encode() if cache_path else None, reps, buf, 2048))
+        return buf.value.decode()
+
+    def launch_count(self):
+        return int(lib().bm_batch_launch_count(self._b))
+
+
+def selftest_barrier(blocks, expect, spin_limit):
+    """(status, timed_out) of the bounded grid-barrier self-test."""
+    t = ctypes.c_int(0)
+    st = lib().bm_selftest_barrier(blocks, expect, spin_limit, ctypes.byref(t))
+    return st, t.value
 
 
 def refine_noalloc(d_u, d_v, d_guide, d_uo, d_vo, width, height, fsize, sEPE, sI, sS, stream=0):

@@ -40,6 +40,7 @@ NVCC_COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ff
 # expressions whose rounding the reference fixes compile to the same instructions.
 ENGINE_UNITS = [
     ("bm_kernels.cu", ["-use_fast_math", "-Xptxas", "-v"]),
+    ("bm_batch.cu", ["-use_fast_math"]),
     ("bm_api.cu", []),
     ("bm_noalloc.cu", []),
     ("bm_params.cpp", []),

@@ -1,0 +1,1038 @@
+// bm_batch.cu -- many frame pairs of uneven size in one pass.
+//
+// A batch packs every pair's buffers into one device arena and describes each pair
+// (geometry, derived constants, buffer addresses) in a device table.  Every stage
+// runs as one launch over the union of all pairs' tiles; a block finds its pair by
+// binary search over per-stage tile prefix sums.  The matching phase (initialisation
+// and every jump-flood level of every iteration) can instead run as one persistent
+// cooperative launch whose blocks meet at a bounded grid barrier between levels.
+// A whole batch step can be captured in a CUDA graph and replayed.  Which schedule
+// runs is chosen by bm_batch_autotune, which times the candidates on the batch
+// itself and caches the winner per batch shape in a JSON file.
+//
+// Each pair is computed exactly as a fresh single-pair context would: the first
+// frame primes, the second is matched with zero initialisation and the random
+// stream positions 0..iterations-1.  The per-pixel bodies are bm_device.cuh's.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "bm_device.cuh"
+
+namespace {
+
+using namespace bmk;
+using namespace bmk::dev;
+
+// One pair of the batch as the kernels see it.
+struct PairDev {
+    int sx, sy, sx_in, sy_in;
+    int P, fsize, tri_s, rmax;
+    float dist, mx, my, cE, cI, cS;
+    int first_up_tile_x;   // tiles per row on the up-sampled grid
+    int first_in_tile_x;   // tiles per row at input resolution (32x8)
+    int first_tri_tile_x;  // tiles per row for the trilateral filter (32x16)
+    const uint8_t* frame[2];
+    float* guide;          // frame 0 as float (the trilateral guide)
+    float* up;
+    uint32_t* F[2];
+    uint32_t* flow[2];
+    uint16_t* cost;
+    float* flow_in;        // U then V
+    float* flow_med;
+    float* flow_out;
+    float* tmp;
+    const int4* pat;
+    const int2* off;
+    const float* taps;
+    const float* lx;
+    const int* ix;
+    const float* ly;
+    const int* iy;
+    const unsigned int* nnx;
+    const unsigned int* nny;
+};
+
+struct BatchDev {
+    const PairDev* pairs;
+    const unsigned int* pre_up;   // [count+1] exclusive prefix of up-sampled-grid tiles
+    const unsigned int* pre_in;   // input-resolution 32x8 tiles
+    const unsigned int* pre_tri;  // trilateral 32x16 tiles
+    int count;
+    int N;
+};
+
+// Bounded grid barrier for the persistent launch (all blocks co-resident by the
+// cooperative launch).  A block that waits longer than `limit` polls sets the error
+// word and every block leaves at its next barrier.
+struct GridSync {
+    unsigned int arrived;
+    unsigned int generation;
+    unsigned int error;
+    unsigned int where;
+};
+
+__device__ __forceinline__ bool grid_sync(GridSync* gs, unsigned int nblocks, unsigned long long limit,
+                                          unsigned int tag)
+{
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        ok = 1;
+        volatile unsigned int* vgen = &gs->generation;
+        volatile unsigned int* verr = &gs->error;
+        const unsigned int gen = *vgen;
+        __threadfence();
+        const unsigned int a = atomicAdd(&gs->arrived, 1u);
+        if (a == nblocks - 1) {
+            atomicExch(&gs->arrived, 0u);
+            __threadfence();
+            atomicAdd(&gs->generation, 1u);
+        } else {
+            unsigned long long it = 0;
+            while (*vgen == gen) {
+                if (*verr || ++it > limit) {
+                    atomicExch(&gs->error, 1u);
+                    atomicMax(&gs->where, tag);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(100);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+__device__ __forceinline__ int find_pair(const unsigned int* __restrict__ pre, int count, unsigned int tile)
+{
+    int lo = 0, hi = count - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(pre + mid) <= tile)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
+// ---------------------------------------------------------------------------
+// Batched stages: blockIdx.x enumerates the union of all pairs' tiles.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_b_guide(BatchDev bd)
+{
+    const unsigned int tile = blockIdx.x;
+    const int i = find_pair(bd.pre_in, bd.count, tile);
+    const PairDev& P = bd.pairs[i];
+    const unsigned int t = tile - bd.pre_in[i];
+    const int x = (int)(t % P.first_in_tile_x) * TX + threadIdx.x, y = (int)(t / P.first_in_tile_x) * TY + threadIdx.y;
+    if (x >= P.sx_in || y >= P.sy_in) return;
+    const size_t o = (size_t)y * P.sx_in + x;
+    P.guide[o] = (float)P.frame[0][o];
+}
+
+__global__ void __launch_bounds__(256) k_b_upsample(BatchDev bd, int which)
+{
+    const unsigned int tile = blockIdx.x;
+    const int i = find_pair(bd.pre_up, bd.count, tile);
+    const PairDev& P = bd.pairs[i];
+    const unsigned int t = tile - bd.pre_up[i];
+    const int x = (int)(t % P.first_up_tile_x) * TX + threadIdx.x, y = (int)(t / P.first_up_tile_x) * TY + threadIdx.y;
+    if (x >= P.sx || y >= P.sy) return;
+    if (P.sx == P.sx_in && P.sy == P.sy_in)
+        P.up[(size_t)y * P.sx + x] = (float)P.frame[which][(size_t)y * P.sx + x];
+    else
+        upsample_px<uint8_t>(P.frame[which], P.up, P.sx_in, P.sy_in, P.sx, P.lx, P.ix, P.ly, P.iy, x, y);
+}
+
+template <int NSP>
+__global__ void __launch_bounds__(256) k_b_features(BatchDev bd, int which)
+{
+    __shared__ int4 s_pat[BM_PATCH_MAX / 4];
+    __shared__ int2 s_off[BM_PATCH_MAX / 4];
+    const unsigned int tile = blockIdx.x;
+    const int i = find_pair(bd.pre_up, bd.count, tile);
+    const PairDev& P = bd.pairs[i];
+    const unsigned int t = tile - bd.pre_up[i];
+    const int bx = (int)(t % P.first_up_tile_x) * TX, by = (int)(t / P.first_up_tile_x) * TY;
+    const int tid = threadIdx.y * TX + threadIdx.x;
+    for (int k = tid; k < NSP * 32; k += TX * TY) {
+        s_off[k] = __ldg(P.off + k);
+        if (k < bd.N) s_pat[k] = __ldg(P.pat + k);
+    }
+    __syncthreads();
+    const int x = bx + threadIdx.x, y = by + threadIdx.y;
+    if (x >= P.sx || y >= P.sy) return;
+    if (tile_interior(bx, by, P.sx, P.sy, P.rmax))
+        features_interior_px<NSP>(P.up, P.F[which], P.sx, x, y, s_off);
+    else
+        features_border_px<NSP>(P.up, P.F[which], P.sx, P.sy, bd.N, s_pat, x, y);
+}
+
+// Tile `tile` of the up-sampled grids, visited in reverse order when rev is set.
+__device__ __forceinline__ bool up_tile(const BatchDev& bd, unsigned int tile, int& i, int& x, int& y)
+{
+    i = find_pair(bd.pre_up, bd.count, tile);
+    const PairDev& P = bd.pairs[i];
+    const unsigned int t = tile - bd.pre_up[i];
+    x = (int)(t % P.first_up_tile_x) * TX + threadIdx.x;
+    y = (int)(t / P.first_up_tile_x) * TY + threadIdx.y;
+    return x < P.sx && y < P.sy;
+}
+
+template <int NSP>
+__global__ void __launch_bounds__(256) k_b_initialize(BatchDev bd, int cur, int rev)
+{
+    const unsigned int total = bd.pre_up[bd.count];
+    const unsigned int tile = rev ? total - 1 - blockIdx.x : blockIdx.x;
+    int i, x, y;
+    if (!up_tile(bd, tile, i, x, y)) return;
+    const PairDev& P = bd.pairs[i];
+    init_px<NSP>(P.F[0], P.F[1], P.flow[cur], P.flow[cur ^ 1], P.cost, P.sx, P.sy, 1, x, y);
+}
+
+template <int NSP, bool RS>
+__global__ void __launch_bounds__(256) k_b_jump(BatchDev bd, int cur, int p, int pd, int doubleProp, RsArgs rs, int rev)
+{
+    const unsigned int total = bd.pre_up[bd.count];
+    const unsigned int tile = rev ? total - 1 - blockIdx.x : blockIdx.x;
+    int i, x, y;
+    if (!up_tile(bd, tile, i, x, y)) return;
+    const PairDev& P = bd.pairs[i];
+    RsArgs r = rs;
+    r.dist = P.dist;
+    jump_px<NSP, RS>(P.F[0], P.F[1], P.flow[cur], P.flow[cur ^ 1], P.cost, P.sx, P.sy, p, pd, doubleProp, r, x, y);
+}
+
+struct MatchPlan {
+    int iterations, jfMax, doubleProp, rng;
+    unsigned long long seed;
+    unsigned long long spin_limit;
+    int snake;
+};
+
+// Initialisation and every jump-flood level of every iteration in one launch.
+// Each phase walks the union of up-sampled tiles with a grid-stride loop, then all
+// blocks meet at the grid barrier before the next phase reads the new field.
+template <int NSP>
+__global__ void __launch_bounds__(256) k_b_match_persistent(BatchDev bd, MatchPlan plan, GridSync* gs)
+{
+    const unsigned int total = bd.pre_up[bd.count];
+    int cur = 0;
+    unsigned int phase = 0;
+    for (unsigned int tile = blockIdx.x; tile < total; tile += gridDim.x) {
+        int i, x, y;
+        if (up_tile(bd, tile, i, x, y)) {
+            const PairDev& P = bd.pairs[i];
+            init_px<NSP>(P.F[0], P.F[1], P.flow[0], P.flow[1], P.cost, P.sx, P.sy, 1, x, y);
+        }
+    }
+    cur = 1;
+    if (!grid_sync(gs, gridDim.x, plan.spin_limit, ++phase)) return;
+    int pd = -1;
+    for (int it = 0; it < plan.iterations; it++) {
+        int levels = 0;
+        for (int s = plan.jfMax; s > 0; s /= 2) levels++;
+        int lvl = 0;
+        for (int s = plan.jfMax; s > 0; s /= 2, lvl++) {
+            const bool last = lvl == levels - 1;
+            const int rev = plan.snake ? (int)(phase & 1u) : 0;
+            RsArgs rs;
+            rs.enabled = last ? 1 : 0;
+            rs.mode = plan.rng;
+            rs.seed = plan.seed;
+            rs.call = (unsigned long long)it;
+            for (unsigned int k = blockIdx.x; k < total; k += gridDim.x) {
+                const unsigned int tile = rev ? total - 1 - k : k;
+                int i, x, y;
+                if (!up_tile(bd, tile, i, x, y)) continue;
+                const PairDev& P = bd.pairs[i];
+                rs.dist = P.dist;
+                if (last)
+                    jump_px<NSP, true, true>(P.F[0], P.F[1], P.flow[cur], P.flow[cur ^ 1], P.cost, P.sx, P.sy, s, pd,
+                                             plan.doubleProp, rs, x, y);
+                else
+                    jump_px<NSP, false, true>(P.F[0], P.F[1], P.flow[cur], P.flow[cur ^ 1], P.cost, P.sx, P.sy, s,
+                                              pd, plan.doubleProp, rs, x, y);
+            }
+            cur ^= 1;
+            if (!grid_sync(gs, gridDim.x, plan.spin_limit, ++phase)) return;
+        }
+        pd = -pd;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_b_downsample(BatchDev bd, int cur)
+{
+    const unsigned int tile = blockIdx.x;
+    const int i = find_pair(bd.pre_in, bd.count, tile);
+    const PairDev& P = bd.pairs[i];
+    const unsigned int t = tile - bd.pre_in[i];
+    const int x = (int)(t % P.first_in_tile_x) * TX + threadIdx.x, y = (int)(t / P.first_in_tile_x) * TY + threadIdx.y;
+    if (x >= P.sx_in || y >= P.sy_in) return;
+    const size_t ni = (size_t)P.sx_in * P.sy_in;
+    if (P.sx == P.sx_in && P.sy == P.sy_in) {
+        const uint32_t f = P.flow[cur][(size_t)y * P.sx + x];
+        P.flow_in[(size_t)y * P.sx_in + x] = (float)lo16(f);
+        P.flow_in[ni + (size_t)y * P.sx_in + x] = (float)hi16(f);
+        return;
+    }
+    downsample_px(P.flow[cur], P.flow_in, P.flow_in + ni, P.sx, P.sy, P.sx_in, P.taps, P.P, P.mx, P.my, P.nnx, P.nny,
+                  x, y);
+}
+
+template <int FS>
+__global__ void __launch_bounds__(256) k_b_median(BatchDev bd, int dir)
+{
+    const unsigned int tile = blockIdx.x;
+    const int i = find_pair(bd.pre_in, bd.count, tile);
+    const PairDev& P = bd.pairs[i];
+    const unsigned int t = tile - bd.pre_in[i];
+    const int x = (int)(t % P.first_in_tile_x) * TX + threadIdx.x, y = (int)(t / P.first_in_tile_x) * TY + threadIdx.y;
+    if (x >= P.sx_in || y >= P.sy_in) return;
+    const size_t ni = (size_t)P.sx_in * P.sy_in;
+    const float* in = dir ? P.flow_in : P.tmp;
+    float* out = dir ? P.tmp : P.flow_med;
+    const int fs = P.fsize == 0 ? 1 : P.fsize;
+    median_px<FS>(in + blockIdx.y * ni, out + blockIdx.y * ni, dir, fs, P.sx_in, P.sy_in, x, y);
+}
+
+__global__ void __launch_bounds__(TX * TRI_TY) k_b_trilateral(BatchDev bd, int filter)
+{
+    extern __shared__ float4 smem4[];
+    const unsigned int tile = blockIdx.x;
+    const int i = find_pair(bd.pre_tri, bd.count, tile);
+    const PairDev& P = bd.pairs[i];
+    const unsigned int t = tile - bd.pre_tri[i];
+    const int bx0 = (int)(t % P.first_tri_tile_x) * TX, by0 = (int)(t / P.first_tri_tile_x) * TRI_BY;
+    const size_t ni = (size_t)P.sx_in * P.sy_in;
+    if (!filter) {
+        for (int r = threadIdx.y; r < TRI_BY; r += TRI_TY) {
+            const int x = bx0 + threadIdx.x, y = by0 + r;
+            if (x < P.sx_in && y < P.sy_in) {
+                const size_t o = (size_t)y * P.sx_in + x;
+                P.flow_out[o] = P.flow_in[o];
+                P.flow_out[ni + o] = P.flow_in[ni + o];
+            }
+        }
+        return;
+    }
+    trilateral_block(P.flow_in, P.flow_in + ni, P.flow_med, P.flow_med + ni, P.guide, P.flow_out, P.flow_out + ni,
+                     P.sx_in, P.sy_in, P.tri_s, P.cE, P.cI, P.cS, bx0, by0, smem4);
+}
+
+// Self-test of the bounded barrier: `blocks` blocks wait for `expect` arrivals.
+__global__ void k_barrier_selftest(GridSync* gs, unsigned int expect, unsigned long long limit)
+{
+    grid_sync(gs, expect, limit, 1);
+}
+
+size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+}  // namespace
+
+struct bm_batch {
+    std::vector<bm_params> prm;
+    uint32_t count = 0;
+    uint32_t N = 0, nsp = 1, iterations = 0, jfMax = 0;
+    int doubleProp = 1, filter = 1, rng = BM_RNG_XORWOW;
+    unsigned long long seed = 0;
+    cudaStream_t own_stream = nullptr, stream = nullptr;
+    char* arena = nullptr;
+    size_t arena_bytes = 0;
+    std::vector<PairDev> pairs;   // host copy (device addresses)
+    PairDev* d_pairs = nullptr;
+    unsigned int* d_pre = nullptr;   // 3 prefix arrays of count+1
+    std::vector<unsigned int> pre_up, pre_in, pre_tri;
+    GridSync* d_sync = nullptr;
+    size_t frames_offset = 0, frames_bytes = 0;   // packed input frames inside the arena
+    size_t flows_offset = 0, flows_bytes = 0;     // packed refined flows (U,V per pair)
+    std::vector<size_t> frame_off, flow_off;
+    int max_fsize = 1, max_tri_s = 0;
+    size_t tri_smem = 0;
+    int coop_blocks_per_sm = 0, num_sms = 0;
+    bm_batch_schedule sched{};
+    cudaGraphExec_t graph_exec = nullptr;
+    cudaGraph_t graph = nullptr;
+    bool graph_valid = false;
+    uint64_t launches = 0;
+};
+
+namespace {
+
+bm_status bfail(bm_status st, const char* fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    bmk::set_error_text(buf);
+    return st;
+}
+
+#define BB_CUDA(call)                                                                                     \
+    do {                                                                                                  \
+        cudaError_t e_ = (call);                                                                          \
+        if (e_ != cudaSuccess) return bfail(BM_ERR_CUDA, "%s (%s:%d)", cudaGetErrorString(e_), __FILE__, __LINE__); \
+    } while (0)
+
+BatchDev batch_dev(const bm_batch* b)
+{
+    BatchDev bd;
+    bd.pairs = b->d_pairs;
+    bd.pre_up = b->d_pre;
+    bd.pre_in = b->d_pre + (b->count + 1);
+    bd.pre_tri = b->d_pre + 2 * (b->count + 1);
+    bd.count = (int)b->count;
+    bd.N = (int)b->N;
+    return bd;
+}
+
+#define BB_NSP(nsp, ...)                                            \
+    switch (nsp) {                                                  \
+    case 1: { constexpr int NSP = 1; __VA_ARGS__; } break;          \
+    case 2: { constexpr int NSP = 2; __VA_ARGS__; } break;          \
+    case 4: { constexpr int NSP = 4; __VA_ARGS__; } break;          \
+    case 8: { constexpr int NSP = 8; __VA_ARGS__; } break;          \
+    case 16: { constexpr int NSP = 16; __VA_ARGS__; } break;        \
+    default: return bfail(BM_ERR_INVALID, "bad descriptor stride"); \
+    }
+
+// Enqueue one batch step on b->stream (no synchronisation).
+bm_status enqueue_step(bm_batch* b, const bm_batch_schedule& s)
+{
+    const BatchDev bd = batch_dev(b);
+    const unsigned int t_up = b->pre_up[b->count], t_in = b->pre_in[b->count], t_tri = b->pre_tri[b->count];
+    cudaStream_t st = b->stream;
+    const dim3 blk(TX, TY);
+    k_b_guide<<<t_in, blk, 0, st>>>(bd);
+    BB_CUDA(cudaGetLastError());
+    for (int which = 0; which < 2; which++) {
+        k_b_upsample<<<t_up, blk, 0, st>>>(bd, which);
+        BB_CUDA(cudaGetLastError());
+        BB_NSP(b->nsp, (k_b_features<NSP><<<t_up, blk, 0, st>>>(bd, which)));
+        BB_CUDA(cudaGetLastError());
+    }
+    b->launches += 5;
+    int cur = 0;
+    if (s.persistent) {
+        BB_CUDA(cudaMemsetAsync(b->d_sync, 0, sizeof(GridSync), st));
+        MatchPlan plan;
+        plan.iterations = (int)b->iterations;
+        plan.jfMax = (int)b->jfMax;
+        plan.doubleProp = b->doubleProp;
+        plan.rng = b->rng;
+        plan.seed = b->seed;
+        plan.spin_limit = s.spin_limit ? s.spin_limit : (1ull << 24);
+        plan.snake = s.snake;
+        const int bps = std::max(1, std::min((int)s.blocks_per_sm, b->coop_blocks_per_sm));
+        const unsigned int grid = std::min<unsigned int>((unsigned)(bps * b->num_sms), t_up);
+        GridSync* gs = b->d_sync;
+        void* args[] = {(void*)&bd, (void*)&plan, (void*)&gs};
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(grid);
+        cfg.blockDim = blk;
+        cfg.stream = st;
+        cudaLaunchAttribute attr;
+        attr.id = cudaLaunchAttributeCooperative;
+        attr.val.cooperative = 1;
+        cfg.attrs = &attr;
+        cfg.numAttrs = 1;
+        cudaError_t e = cudaSuccess;
+        BB_NSP(b->nsp, (e = cudaLaunchKernelExC(&cfg, (const void*)k_b_match_persistent<NSP>, args)));
+        BB_CUDA(e);
+        b->launches += 1;
+        int levels = 0;
+        for (int q = (int)b->jfMax; q > 0; q /= 2) levels++;
+        cur = (1 + (int)b->iterations * levels) & 1;
+    } else {
+        int rev = 0;
+        BB_NSP(b->nsp, (k_b_initialize<NSP><<<t_up, blk, 0, st>>>(bd, cur, rev)));
+        BB_CUDA(cudaGetLastError());
+        b->launches++;
+        cur ^= 1;
+        int pd = -1;
+        for (uint32_t it = 0; it < b->iterations; it++) {
+            int levels = 0;
+            for (int q = (int)b->jfMax; q > 0; q /= 2) levels++;
+            int lvl = 0;
+            for (int q = (int)b->jfMax; q > 0; q /= 2, lvl++) {
+                rev = s.snake ? rev ^ 1 : 0;
+                RsArgs rs;
+                rs.enabled = lvl == levels - 1;
+                rs.mode = b->rng;
+                rs.seed = b->seed;
+                rs.call = it;
+                rs.dist = 0;
+                if (rs.enabled) {
+                    BB_NSP(b->nsp, (k_b_jump<NSP, true><<<t_up, blk, 0, st>>>(bd, cur, q, pd, b->doubleProp, rs, rev)));
+                } else {
+                    BB_NSP(b->nsp, (k_b_jump<NSP, false><<<t_up, blk, 0, st>>>(bd, cur, q, pd, b->doubleProp, rs, rev)));
+                }
+                BB_CUDA(cudaGetLastError());
+                b->launches++;
+                cur ^= 1;
+            }
+            pd = -pd;
+        }
+    }
+    k_b_downsample<<<t_in, blk, 0, st>>>(bd, cur);
+    BB_CUDA(cudaGetLastError());
+    if (b->filter) {
+        const dim3 g2(t_in, 2);
+#define BB_MED(FSV)                                                        \
+    do {                                                                   \
+        k_b_median<FSV><<<g2, blk, 0, st>>>(bd, 1);                        \
+        k_b_median<FSV><<<g2, blk, 0, st>>>(bd, 0);                        \
+    } while (0)
+        if (b->max_fsize <= 9) BB_MED(9);
+        else if (b->max_fsize <= 13) BB_MED(13);
+        else if (b->max_fsize <= 15) BB_MED(15);
+        else if (b->max_fsize <= 23) BB_MED(23);
+        else if (b->max_fsize <= 31) BB_MED(31);
+        else BB_MED(BM_MAX_MEDIAN);
+#undef BB_MED
+        BB_CUDA(cudaGetLastError());
+        b->launches += 2;
+    }
+    k_b_trilateral<<<t_tri, dim3(TX, TRI_TY), b->filter ? b->tri_smem : 0, st>>>(bd, b->filter);
+    BB_CUDA(cudaGetLastError());
+    b->launches += 2;
+    return BM_OK;
+}
+
+void destroy_graph(bm_batch* b)
+{
+    if (b->graph_exec) cudaGraphExecDestroy(b->graph_exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->graph_exec = nullptr;
+    b->graph = nullptr;
+    b->graph_valid = false;
+}
+
+bm_status capture_graph(bm_batch* b)
+{
+    destroy_graph(b);
+    BB_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    bm_status st = enqueue_step(b, b->sched);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+    if (st != BM_OK) {
+        if (g) cudaGraphDestroy(g);
+        return st;
+    }
+    if (e != cudaSuccess) return bfail(BM_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+    b->graph = g;
+    e = cudaGraphInstantiate(&b->graph_exec, g, 0);
+    if (e != cudaSuccess) {
+        destroy_graph(b);
+        return bfail(BM_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+    }
+    b->graph_valid = true;
+    return BM_OK;
+}
+
+bm_status check_sync(bm_batch* b)
+{
+    if (!b->sched.persistent) return BM_OK;
+    GridSync h;
+    BB_CUDA(cudaMemcpyAsync(&h, b->d_sync, sizeof(h), cudaMemcpyDeviceToHost, b->stream));
+    BB_CUDA(cudaStreamSynchronize(b->stream));
+    if (h.error) return bfail(BM_ERR_TIMEOUT, "batched matching: a grid barrier timed out (phase %u)", h.where);
+    return BM_OK;
+}
+
+std::string shape_key(const bm_batch* b)
+{
+    unsigned long long px = 0;
+    for (const auto& p : b->prm) px += (unsigned long long)p.sx * p.sy;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceProp prop;
+    cudaGetDeviceProperties(&prop, dev);
+    std::ostringstream ss;
+    ss << prop.name << "|pairs=" << b->count << "|N=" << b->N << "|it=" << b->iterations << "|jf=" << b->jfMax
+       << "|upMpx=" << (px + 500000) / 1000000;
+    return ss.str();
+}
+
+}  // namespace
+
+extern "C" {
+
+bm_status bm_batch_create(const bm_params* pairs, uint32_t count, bm_batch** out)
+{
+    if (!pairs || !out || count == 0) return bfail(BM_ERR_INVALID, "bm_batch_create: empty batch");
+    *out = nullptr;
+    const bm_params& p0 = pairs[0];
+    for (uint32_t i = 0; i < count; i++) {
+        const bm_params& p = pairs[i];
+        if (p.N != p0.N || p.iterations != p0.iterations || p.jfMax != p0.jfMax || p.doubleProp != p0.doubleProp ||
+            p.filter != p0.filter || p.rng != p0.rng || p.seed != p0.seed)
+            return bfail(BM_ERR_INVALID, "bm_batch_create: pair %u differs in N/iterations/jfMax/doubleProp/filter/rng",
+                         i);
+        if (p.N < 1 || p.N > BM_PATCH_MAX / 4 || p.fsize > BM_MAX_MEDIAN || p.sx == 0 || p.sy == 0 || p.sx_in == 0 ||
+            p.sy_in == 0 || p.sx > 32767 || p.sy > 32767)
+            return bfail(BM_ERR_LIMIT, "bm_batch_create: pair %u has parameters beyond the limits", i);
+        if (std::ceil(p.sigma * 3) * 2 + 1 > BM_CONST_KERNEL_SIZE)
+            return bfail(BM_ERR_LIMIT, "bm_batch_create: pair %u: Gaussian down-sampling filter too large", i);
+    }
+    bm_batch* b = new bm_batch();
+    b->prm.assign(pairs, pairs + count);
+    b->count = count;
+    b->N = p0.N;
+    b->nsp = feature_stride(p0.N);
+    b->iterations = p0.iterations;
+    b->jfMax = p0.jfMax;
+    b->doubleProp = p0.doubleProp ? 1 : 0;
+    b->filter = p0.filter ? 1 : 0;
+    b->rng = (int)p0.rng;
+    b->seed = p0.seed;
+    b->sched.persistent = 0;
+    b->sched.blocks_per_sm = 0;
+    b->sched.snake = 1;
+    b->sched.use_graph = 1;
+    b->sched.spin_limit = 1ull << 24;
+
+    // layout
+    struct Off {
+        size_t frame[2], guide, up, F[2], flow[2], cost, fin, fmed, fout, tmp, pat, off, taps, lx, ix, ly, iy, nnx, nny;
+    };
+    std::vector<Off> offs(count);
+    size_t cursor = 0;
+    auto take = [&](size_t bytes) {
+        const size_t o = cursor;
+        cursor += align256(bytes);
+        return o;
+    };
+    // packed inputs first (pair-major, frame 0 then frame 1) and packed outputs next,
+    // so the e2e path moves each with one copy
+    b->frames_offset = 0;
+    b->frame_off.resize(2 * (size_t)count);
+    size_t fcur = 0;
+    for (uint32_t i = 0; i < count; i++)
+        for (int k = 0; k < 2; k++) {
+            b->frame_off[2 * i + k] = fcur;
+            fcur += (size_t)pairs[i].sx_in * pairs[i].sy_in;
+        }
+    b->frames_bytes = fcur;
+    cursor = align256(fcur);
+    b->flows_offset = cursor;
+    b->flow_off.resize(count);
+    size_t ocur = 0;
+    for (uint32_t i = 0; i < count; i++) {
+        b->flow_off[i] = ocur;
+        ocur += 2 * (size_t)pairs[i].sx_in * pairs[i].sy_in * sizeof(float);
+    }
+    b->flows_bytes = ocur;
+    cursor += align256(ocur);
+    for (uint32_t i = 0; i < count; i++) {
+        const bm_params& p = pairs[i];
+        const size_t n = (size_t)p.sx * p.sy, ni = (size_t)p.sx_in * p.sy_in;
+        Off& o = offs[i];
+        o.guide = take(ni * 4);
+        o.up = take(n * 4);
+        o.F[0] = take(n * b->nsp * 4);
+        o.F[1] = take(n * b->nsp * 4);
+        o.flow[0] = take(n * 4);
+        o.flow[1] = take(n * 4);
+        o.cost = take(n * 2);
+        o.fin = take(2 * ni * 4);
+        o.fmed = take(2 * ni * 4);
+        o.tmp = take(2 * ni * 4);
+        o.pat = take((BM_PATCH_MAX / 4) * sizeof(int4));
+        o.off = take((BM_PATCH_MAX / 4) * sizeof(int2));
+        o.taps = take(BM_CONST_KERNEL_SIZE * 4);
+        o.lx = take((size_t)p.sx * 6 * 4);
+        o.ix = take((size_t)p.sx * 4);
+        o.ly = take((size_t)p.sy * 6 * 4);
+        o.iy = take((size_t)p.sy * 4);
+        o.nnx = take((size_t)p.sx_in * 4);
+        o.nny = take((size_t)p.sy_in * 4);
+    }
+    b->arena_bytes = cursor;
+    cudaError_t e = cudaMalloc((void**)&b->arena, b->arena_bytes);
+    if (e != cudaSuccess) {
+        delete b;
+        return bfail(BM_ERR_NOMEM, "bm_batch_create: cudaMalloc of %zu bytes failed: %s", cursor, cudaGetErrorString(e));
+    }
+    e = cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        cudaFree(b->arena);
+        delete b;
+        return bfail(BM_ERR_CUDA, "bm_batch_create: %s", cudaGetErrorString(e));
+    }
+    b->stream = b->own_stream;
+    auto fail_clean = [&](bm_status st) {
+        bm_batch_destroy(b);
+        return st;
+    };
+    if (cudaMemsetAsync(b->arena, 0, b->arena_bytes, b->stream) != cudaSuccess)
+        return fail_clean(bfail(BM_ERR_CUDA, "bm_batch_create: clearing the arena failed"));
+    // tiles and descriptors
+    b->pairs.resize(count);
+    b->pre_up.assign(count + 1, 0);
+    b->pre_in.assign(count + 1, 0);
+    b->pre_tri.assign(count + 1, 0);
+    std::vector<float> pattern(4 * (size_t)b->N);
+    for (uint32_t i = 0; i < count; i++) {
+        const bm_params& p = pairs[i];
+        const Off& o = offs[i];
+        PairDev& d = b->pairs[i];
+        d.sx = (int)p.sx;
+        d.sy = (int)p.sy;
+        d.sx_in = (int)p.sx_in;
+        d.sy_in = (int)p.sy_in;
+        float taps[BM_CONST_KERNEL_SIZE];
+        uint32_t P = 0;
+        bm_gauss_taps(p.sigma, taps, &P);
+        d.P = (int)P;
+        d.fsize = (int)p.fsize;
+        d.tri_s = (int)std::ceil(2.5 * (double)std::sqrt(p.sS * p.sS));
+        d.dist = std::sqrt(std::ceil((float)p.sx * 0.5f / 3.0f));
+        d.mx = (float)p.sx_in / (float)p.sx;
+        d.my = (float)p.sy_in / (float)p.sy;
+        const TriCoef tc = tri_coef(p.sEPE * p.sEPE, p.sI * p.sI, p.sS * p.sS);
+        d.cE = tc.cE;
+        d.cI = tc.cI;
+        d.cS = tc.cS;
+        d.first_up_tile_x = (d.sx + TX - 1) / TX;
+        d.first_in_tile_x = (d.sx_in + TX - 1) / TX;
+        d.first_tri_tile_x = (d.sx_in + TX - 1) / TX;
+        b->pre_up[i + 1] = b->pre_up[i] + (unsigned)(d.first_up_tile_x * ((d.sy + TY - 1) / TY));
+        b->pre_in[i + 1] = b->pre_in[i] + (unsigned)(d.first_in_tile_x * ((d.sy_in + TY - 1) / TY));
+        b->pre_tri[i + 1] = b->pre_tri[i] + (unsigned)(d.first_tri_tile_x * ((d.sy_in + TRI_BY - 1) / TRI_BY));
+        char* A = b->arena;
+        d.frame[0] = reinterpret_cast<const uint8_t*>(A + b->frames_offset + b->frame_off[2 * i]);
+        d.frame[1] = reinterpret_cast<const uint8_t*>(A + b->frames_offset + b->frame_off[2 * i + 1]);
+        d.flow_out = reinterpret_cast<float*>(A + b->flows_offset + b->flow_off[i]);
+        d.guide = reinterpret_cast<float*>(A + o.guide);
+        d.up = reinterpret_cast<float*>(A + o.up);
+        d.F[0] = reinterpret_cast<uint32_t*>(A + o.F[0]);
+        d.F[1] = reinterpret_cast<uint32_t*>(A + o.F[1]);
+        d.flow[0] = reinterpret_cast<uint32_t*>(A + o.flow[0]);
+        d.flow[1] = reinterpret_cast<uint32_t*>(A + o.flow[1]);
+        d.cost = reinterpret_cast<uint16_t*>(A + o.cost);
+        d.flow_in = reinterpret_cast<float*>(A + o.fin);
+        d.flow_med = reinterpret_cast<float*>(A + o.fmed);
+        d.tmp = reinterpret_cast<float*>(A + o.tmp);
+        d.pat = reinterpret_cast<const int4*>(A + o.pat);
+        d.off = reinterpret_cast<const int2*>(A + o.off);
+        d.taps = reinterpret_cast<const float*>(A + o.taps);
+        d.lx = reinterpret_cast<const float*>(A + o.lx);
+        d.ix = reinterpret_cast<const int*>(A + o.ix);
+        d.ly = reinterpret_cast<const float*>(A + o.ly);
+        d.iy = reinterpret_cast<const int*>(A + o.iy);
+        d.nnx = reinterpret_cast<const unsigned int*>(A + o.nnx);
+        d.nny = reinterpret_cast<const unsigned int*>(A + o.nny);
+        b->max_fsize = std::max(b->max_fsize, (int)p.fsize);
+        b->max_tri_s = std::max(b->max_tri_s, d.tri_s);
+        if (cudaMemcpyAsync((void*)d.taps, taps, P * sizeof(float), cudaMemcpyHostToDevice, b->stream) != cudaSuccess ||
+            lanczos_tables((float*)d.lx, (int*)d.ix, d.sx_in, d.sx, b->stream) != cudaSuccess ||
+            lanczos_tables((float*)d.ly, (int*)d.iy, d.sy_in, d.sy, b->stream) != cudaSuccess ||
+            nn_table((unsigned int*)d.nnx, d.sx, d.sx_in, b->stream) != cudaSuccess ||
+            nn_table((unsigned int*)d.nny, d.sy, d.sy_in, b->stream) != cudaSuccess)
+            return fail_clean(bfail(BM_ERR_CUDA, "bm_batch_create: table set-up failed"));
+        bm_make_pattern(&p, 0, pattern.data());
+        bm_status st = bm_batch_set_pattern(b, i, pattern.data(), 4 * b->N);
+        if (st != BM_OK) return fail_clean(st);
+    }
+    b->tri_smem = tri_smem_bytes(b->max_tri_s);
+    if (b->filter && b->tri_smem > 220 * 1024)
+        return fail_clean(bfail(BM_ERR_LIMIT, "bm_batch_create: spatial window %d too large for the batched filter",
+                                b->max_tri_s));
+    if (cudaMalloc((void**)&b->d_pairs, count * sizeof(PairDev)) != cudaSuccess ||
+        cudaMalloc((void**)&b->d_pre, 3 * (count + 1) * sizeof(unsigned int)) != cudaSuccess ||
+        cudaMalloc((void**)&b->d_sync, sizeof(GridSync)) != cudaSuccess)
+        return fail_clean(bfail(BM_ERR_NOMEM, "bm_batch_create: descriptor allocation failed"));
+    std::vector<unsigned int> pre;
+    pre.insert(pre.end(), b->pre_up.begin(), b->pre_up.end());
+    pre.insert(pre.end(), b->pre_in.begin(), b->pre_in.end());
+    pre.insert(pre.end(), b->pre_tri.begin(), b->pre_tri.end());
+    if (cudaMemcpyAsync(b->d_pairs, b->pairs.data(), count * sizeof(PairDev), cudaMemcpyHostToDevice, b->stream) !=
+            cudaSuccess ||
+        cudaMemcpyAsync(b->d_pre, pre.data(), pre.size() * sizeof(unsigned int), cudaMemcpyHostToDevice, b->stream) !=
+            cudaSuccess ||
+        cudaMemsetAsync(b->d_sync, 0, sizeof(GridSync), b->stream) != cudaSuccess ||
+        cudaStreamSynchronize(b->stream) != cudaSuccess)
+        return fail_clean(bfail(BM_ERR_CUDA, "bm_batch_create: descriptor upload failed"));
+    if (b->tri_smem > 48 * 1024 &&
+        cudaFuncSetAttribute(k_b_trilateral, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->tri_smem) !=
+            cudaSuccess)
+        return fail_clean(bfail(BM_ERR_CUDA, "bm_batch_create: shared-memory opt-in failed"));
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&b->num_sms, cudaDevAttrMultiProcessorCount, dev);
+    int occ = 0;
+    cudaError_t oe = cudaSuccess;
+    switch (b->nsp) {
+    case 1: oe = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_b_match_persistent<1>, TX * TY, 0); break;
+    case 2: oe = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_b_match_persistent<2>, TX * TY, 0); break;
+    case 4: oe = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_b_match_persistent<4>, TX * TY, 0); break;
+    case 8: oe = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_b_match_persistent<8>, TX * TY, 0); break;
+    default: oe = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_b_match_persistent<16>, TX * TY, 0); break;
+    }
+    if (oe != cudaSuccess) return fail_clean(bfail(BM_ERR_CUDA, "occupancy query: %s", cudaGetErrorString(oe)));
+    b->coop_blocks_per_sm = occ;
+    b->sched.blocks_per_sm = (uint32_t)occ;
+    *out = b;
+    return BM_OK;
+}
+
+bm_status bm_batch_destroy(bm_batch* b)
+{
+    if (!b) return BM_OK;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    destroy_graph(b);
+    if (b->arena) cudaFree(b->arena);
+    if (b->d_pairs) cudaFree(b->d_pairs);
+    if (b->d_pre) cudaFree(b->d_pre);
+    if (b->d_sync) cudaFree(b->d_sync);
+    if (b->own_stream) cudaStreamDestroy(b->own_stream);
+    delete b;
+    return BM_OK;
+}
+
+uint32_t bm_batch_count(const bm_batch* b) { return b ? b->count : 0; }
+
+bm_status bm_batch_set_stream(bm_batch* b, void* stream)
+{
+    if (!b) return bfail(BM_ERR_INVALID, "null batch");
+    cudaStream_t s = stream ? (cudaStream_t)stream : b->own_stream;
+    if (s != b->stream) destroy_graph(b);
+    b->stream = s;
+    return BM_OK;
+}
+
+bm_status bm_batch_set_pattern(bm_batch* b, uint32_t pair, const float* h_pattern, uint32_t count)
+{
+    if (!b || !h_pattern || pair >= b->count) return bfail(BM_ERR_INVALID, "bm_batch_set_pattern: bad argument");
+    if (count != 4 * b->N) return bfail(BM_ERR_INVALID, "bm_batch_set_pattern: expected 4*N values");
+    std::vector<int4> pat(b->N);
+    std::vector<int2> off(BM_PATCH_MAX / 4, make_int2(0, 0));
+    int rmax = 0;
+    const int sx = b->pairs[pair].sx;
+    for (uint32_t s = 0; s < b->N; s++) {
+        int v[4];
+        for (int k = 0; k < 4; k++) {
+            v[k] = (int)h_pattern[4 * s + k];
+            rmax = std::max(rmax, std::abs(v[k]));
+        }
+        pat[s] = make_int4(v[0], v[1], v[2], v[3]);
+        off[s] = make_int2(v[0] + v[1] * sx, v[2] + v[3] * sx);
+    }
+    PairDev& d = b->pairs[pair];
+    d.rmax = rmax;
+    BB_CUDA(cudaMemcpyAsync((void*)d.pat, pat.data(), b->N * sizeof(int4), cudaMemcpyHostToDevice, b->stream));
+    BB_CUDA(cudaMemcpyAsync((void*)d.off, off.data(), off.size() * sizeof(int2), cudaMemcpyHostToDevice, b->stream));
+    if (b->d_pairs)
+        BB_CUDA(cudaMemcpyAsync(b->d_pairs + pair, &d, sizeof(PairDev), cudaMemcpyHostToDevice, b->stream));
+    BB_CUDA(cudaStreamSynchronize(b->stream));
+    return BM_OK;
+}
+
+bm_status bm_batch_frame_ptr(bm_batch* b, uint32_t pair, uint32_t which, uint8_t** d_ptr)
+{
+    if (!b || !d_ptr || pair >= b->count || which > 1) return bfail(BM_ERR_INVALID, "bm_batch_frame_ptr: bad argument");
+    *d_ptr = reinterpret_cast<uint8_t*>(b->arena + b->frames_offset + b->frame_off[2 * pair + which]);
+    return BM_OK;
+}
+
+bm_status bm_batch_load_frames(bm_batch* b, const uint8_t* packed, size_t bytes, int on_device)
+{
+    if (!b || !packed) return bfail(BM_ERR_INVALID, "bm_batch_load_frames: null argument");
+    if (bytes != b->frames_bytes)
+        return bfail(BM_ERR_INVALID, "bm_batch_load_frames: expected %zu bytes, got %zu", b->frames_bytes, bytes);
+    BB_CUDA(cudaMemcpyAsync(b->arena + b->frames_offset, packed, bytes,
+                            on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, b->stream));
+    return BM_OK;
+}
+
+size_t bm_batch_frames_bytes(const bm_batch* b) { return b ? b->frames_bytes : 0; }
+size_t bm_batch_flows_bytes(const bm_batch* b) { return b ? b->flows_bytes : 0; }
+
+bm_status bm_batch_read_flows(bm_batch* b, float* packed, size_t bytes, int on_device)
+{
+    if (!b || !packed) return bfail(BM_ERR_INVALID, "bm_batch_read_flows: null argument");
+    if (bytes != b->flows_bytes)
+        return bfail(BM_ERR_INVALID, "bm_batch_read_flows: expected %zu bytes, got %zu", b->flows_bytes, bytes);
+    BB_CUDA(cudaMemcpyAsync(packed, b->arena + b->flows_offset, bytes,
+                            on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, b->stream));
+    if (!on_device) BB_CUDA(cudaStreamSynchronize(b->stream));
+    return BM_OK;
+}
+
+bm_status bm_batch_flow_ptr(bm_batch* b, uint32_t pair, float** d_u, float** d_v)
+{
+    if (!b || pair >= b->count || !d_u || !d_v) return bfail(BM_ERR_INVALID, "bm_batch_flow_ptr: bad argument");
+    const size_t ni = (size_t)b->pairs[pair].sx_in * b->pairs[pair].sy_in;
+    *d_u = b->pairs[pair].flow_out;
+    *d_v = b->pairs[pair].flow_out + ni;
+    return BM_OK;
+}
+
+bm_status bm_batch_set_schedule(bm_batch* b, const bm_batch_schedule* s)
+{
+    if (!b || !s) return bfail(BM_ERR_INVALID, "bm_batch_set_schedule: null argument");
+    b->sched = *s;
+    if (b->sched.blocks_per_sm == 0 || (int)b->sched.blocks_per_sm > b->coop_blocks_per_sm)
+        b->sched.blocks_per_sm = (uint32_t)b->coop_blocks_per_sm;
+    destroy_graph(b);
+    return BM_OK;
+}
+
+bm_status bm_batch_get_schedule(const bm_batch* b, bm_batch_schedule* s)
+{
+    if (!b || !s) return bfail(BM_ERR_INVALID, "bm_batch_get_schedule: null argument");
+    *s = b->sched;
+    return BM_OK;
+}
+
+bm_status bm_batch_run(bm_batch* b)
+{
+    if (!b) return bfail(BM_ERR_INVALID, "null batch");
+    if (b->sched.use_graph) {
+        if (!b->graph_valid) {
+            bm_status st = capture_graph(b);
+            if (st != BM_OK) return st;
+        }
+        BB_CUDA(cudaGraphLaunch(b->graph_exec, b->stream));
+    } else {
+        bm_status st = enqueue_step(b, b->sched);
+        if (st != BM_OK) return st;
+    }
+    return BM_OK;
+}
+
+bm_status bm_batch_synchronize(bm_batch* b)
+{
+    if (!b) return bfail(BM_ERR_INVALID, "null batch");
+    BB_CUDA(cudaStreamSynchronize(b->stream));
+    return check_sync(b);
+}
+
+uint64_t bm_batch_launch_count(const bm_batch* b) { return b ? b->launches : 0; }
+
+// Times each candidate schedule on this batch (after one untimed run each) and keeps
+// the fastest; with cache_path, a previous choice for the same shape is reused and
+// new choices are appended (one JSON object per line: {"key": ..., schedule, "ms"}).
+bm_status bm_batch_autotune(bm_batch* b, const char* cache_path, int reps, char* report, size_t report_len)
+{
+    if (!b) return bfail(BM_ERR_INVALID, "null batch");
+    const std::string key = shape_key(b);
+    if (cache_path) {
+        std::ifstream in(cache_path);
+        std::string line, hit;
+        while (std::getline(in, line))
+            if (line.find("\"key\": \"" + key + "\"") != std::string::npos) hit = line;
+        if (!hit.empty()) {
+            bm_batch_schedule s = b->sched;
+            unsigned long long v;
+            auto grab = [&](const char* name, unsigned long long& dst) {
+                const std::string k = std::string("\"") + name + "\": ";
+                const size_t pos = hit.find(k);
+                if (pos == std::string::npos) return false;
+                dst = std::strtoull(hit.c_str() + pos + k.size(), nullptr, 10);
+                return true;
+            };
+            bool ok = true;
+            ok &= grab("persistent", v) && ((s.persistent = (uint32_t)v), true);
+            ok &= grab("blocks_per_sm", v) && ((s.blocks_per_sm = (uint32_t)v), true);
+            ok &= grab("snake", v) && ((s.snake = (uint32_t)v), true);
+            ok &= grab("use_graph", v) && ((s.use_graph = (uint32_t)v), true);
+            if (ok) {
+                bm_batch_set_schedule(b, &s);
+                if (report) std::snprintf(report, report_len, "cached: %s", hit.c_str());
+                return BM_OK;
+            }
+        }
+    }
+    std::vector<bm_batch_schedule> cands;
+    for (uint32_t snake = 0; snake <= 1; snake++) {
+        bm_batch_schedule s = b->sched;
+        s.persistent = 0;
+        s.snake = snake;
+        s.use_graph = 1;
+        cands.push_back(s);
+    }
+    for (int bps : {b->coop_blocks_per_sm, std::max(1, b->coop_blocks_per_sm / 2)}) {
+        bm_batch_schedule s = b->sched;
+        s.persistent = 1;
+        s.blocks_per_sm = (uint32_t)bps;
+        s.snake = 1;
+        s.use_graph = 1;
+        cands.push_back(s);
+    }
+    if (reps < 1) reps = 3;
+    double best_ms = 1e30;
+    bm_batch_schedule best = b->sched;
+    std::ostringstream rep;
+    cudaEvent_t e0, e1;
+    BB_CUDA(cudaEventCreate(&e0));
+    BB_CUDA(cudaEventCreate(&e1));
+    for (const auto& s : cands) {
+        bm_batch_set_schedule(b, &s);
+        bm_status st = bm_batch_run(b);
+        if (st == BM_OK) st = bm_batch_synchronize(b);
+        if (st != BM_OK) {
+            rep << "{persistent=" << s.persistent << ",bps=" << s.blocks_per_sm << ",snake=" << s.snake
+                << ": failed} ";
+            continue;
+        }
+        cudaEventRecord(e0, b->stream);
+        for (int r = 0; r < reps && st == BM_OK; r++) st = bm_batch_run(b);
+        cudaEventRecord(e1, b->stream);
+        if (st == BM_OK) st = bm_batch_synchronize(b);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        ms /= reps;
+        rep << "{persistent=" << s.persistent << ",bps=" << s.blocks_per_sm << ",snake=" << s.snake << ": "
+            << (st == BM_OK ? std::to_string(ms) : std::string("failed")) << " ms} ";
+        if (st == BM_OK && ms < best_ms) {
+            best_ms = ms;
+            best = s;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    bm_batch_set_schedule(b, &best);
+    if (cache_path) {
+        std::ofstream out(cache_path, std::ios::app);
+        out << "{\"key\": \"" << key << "\", \"persistent\": " << best.persistent << ", \"blocks_per_sm\": "
+            << best.blocks_per_sm << ", \"snake\": " << best.snake << ", \"use_graph\": " << best.use_graph
+            << ", \"ms\": " << best_ms << "}\n";
+    }
+    if (report) std::snprintf(report, report_len, "%s-> persistent=%u bps=%u snake=%u", rep.str().c_str(),
+                              best.persistent, best.blocks_per_sm, best.snake);
+    return BM_OK;
+}
+
+bm_status bm_selftest_barrier(uint32_t blocks, uint32_t expect, uint64_t spin_limit, int* timed_out)
+{
+    if (!timed_out || blocks == 0 || blocks > 64) return bfail(BM_ERR_INVALID, "bm_selftest_barrier: bad argument");
+    GridSync* gs = nullptr;
+    BB_CUDA(cudaMalloc((void**)&gs, sizeof(GridSync)));
+    cudaMemset(gs, 0, sizeof(GridSync));
+    void* args[] = {(void*)&gs, (void*)&expect, (void*)&spin_limit};
+    cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_barrier_selftest, dim3(blocks), dim3(32), args, 0, 0);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    GridSync h{};
+    if (e == cudaSuccess) e = cudaMemcpy(&h, gs, sizeof(h), cudaMemcpyDeviceToHost);
+    cudaFree(gs);
+    if (e != cudaSuccess) return bfail(BM_ERR_CUDA, "bm_selftest_barrier: %s", cudaGetErrorString(e));
+    *timed_out = h.error ? 1 : 0;
+    return h.error ? bfail(BM_ERR_TIMEOUT, "grid barrier gave up after %llu polls", (unsigned long long)spin_limit)
+                   : BM_OK;
+}
+
+}  // extern "C"

@@ -192,6 +192,55 @@ bm_status bm_nn_indices(bm_ctx* ctx, uint32_t* h_x, uint32_t* h_y);
 bm_status bm_rng_position(bm_ctx* ctx, uint64_t* calls);
 bm_status bm_set_rng_position(bm_ctx* ctx, uint64_t calls);
 
+/* ---- many pairs at once ------------------------------------------------------------ */
+
+/* A batch of frame pairs of uneven size (no counterpart in the reference, which
+ * processes one pair at a time).  Every pair is computed exactly as a fresh context
+ * would compute it (bm_create, then bm_frame on its first and second frame); all
+ * pairs must share N, iterations, jfMax, doubleProp, filter and the random stream.
+ * Each stage runs as one launch over the union of all pairs' tiles; the matching
+ * phase can run as one persistent cooperative launch with bounded grid barriers; a
+ * whole step can be captured in a CUDA graph.  Frames and flows are packed in pair
+ * order: frames = pair0 frame0, pair0 frame1, pair1 frame0, ... (uint8, sx_in*sy_in
+ * each); flows = pair0 U, pair0 V, pair1 U, ... (float). */
+typedef struct bm_batch bm_batch;
+
+typedef struct bm_batch_schedule {
+    uint32_t persistent;     /* matching phase as one persistent launch */
+    uint32_t blocks_per_sm;  /* resident blocks per SM of the persistent launch (0 = maximum) */
+    uint32_t snake;          /* alternate the tile order between passes */
+    uint32_t use_graph;      /* capture the step in a CUDA graph and replay it */
+    uint64_t spin_limit;     /* polls before a grid barrier gives up (BM_ERR_TIMEOUT) */
+} bm_batch_schedule;
+
+bm_status bm_batch_create(const bm_params* pairs, uint32_t count, bm_batch** out);
+bm_status bm_batch_destroy(bm_batch* b);
+uint32_t bm_batch_count(const bm_batch* b);
+bm_status bm_batch_set_stream(bm_batch* b, void* stream);
+bm_status bm_batch_set_pattern(bm_batch* b, uint32_t pair, const float* h_pattern, uint32_t count);
+size_t bm_batch_frames_bytes(const bm_batch* b);
+size_t bm_batch_flows_bytes(const bm_batch* b);
+bm_status bm_batch_frame_ptr(bm_batch* b, uint32_t pair, uint32_t which, uint8_t** d_ptr);
+bm_status bm_batch_load_frames(bm_batch* b, const uint8_t* packed, size_t bytes, int on_device);
+bm_status bm_batch_read_flows(bm_batch* b, float* packed, size_t bytes, int on_device);
+bm_status bm_batch_flow_ptr(bm_batch* b, uint32_t pair, float** d_u, float** d_v);
+bm_status bm_batch_set_schedule(bm_batch* b, const bm_batch_schedule* s);
+bm_status bm_batch_get_schedule(const bm_batch* b, bm_batch_schedule* s);
+/* Queue one step (all pairs) on the batch stream. */
+bm_status bm_batch_run(bm_batch* b);
+/* Wait for the step; BM_ERR_TIMEOUT if a grid barrier of the persistent launch gave up. */
+bm_status bm_batch_synchronize(bm_batch* b);
+uint64_t bm_batch_launch_count(const bm_batch* b);
+/* Time the candidate schedules on this batch and keep the fastest.  cache_path (may be
+ * NULL) is a file of JSON lines keyed by GPU and batch shape: a cached choice is reused
+ * without timing, a new one is appended.  report receives a one-line summary. */
+bm_status bm_batch_autotune(bm_batch* b, const char* cache_path, int reps, char* report, size_t report_len);
+
+/* Self-test of the bounded grid barrier: `blocks` co-resident blocks wait for `expect`
+ * arrivals for at most spin_limit polls each.  With expect > blocks nobody can pass:
+ * every block gives up, *timed_out is set and BM_ERR_TIMEOUT returned. */
+bm_status bm_selftest_barrier(uint32_t blocks, uint32_t expect, uint64_t spin_limit, int* timed_out);
+
 /* ---- refinement without allocation ------------------------------------------------ */
 
 /* No counterpart in the reference.  The refinement of bm_process (median filter

@@ -1,0 +1,105 @@
+"""Batched pairs of uneven size: every pair of a batch equals a fresh single-pair
+context on the same frames (bit for bit), for every schedule; the autotuner and
+its cache; the bounded grid barrier gives up instead of hanging."""
+from __future__ import annotations
+
+import json
+
+import numpy as np
+import pytest
+
+import briefmatch_gb300 as bm
+from briefmatch_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("no GPU", allow_module_level=True)
+
+SIZES = [(96, 64), (130, 70), (64, 64), (200, 124), (77, 53)]
+
+
+def _batch_inputs(u=2.0, N=64):
+    params = [bm.BMParams.derive(w, h, u, u, N=N) for w, h in SIZES]
+    frames = [synth.make_pair(20 + k, w, h, 5.0)[:2] for k, (w, h) in enumerate(SIZES)]
+    return params, frames
+
+
+def _single(params, frames):
+    outs = []
+    for p, (f0, f1) in zip(params, frames):
+        eng = bm.FlowEngine(p)
+        eng.process_frame(f0)
+        outs.append(eng.process_frame(f1))
+        eng.clean()
+    return outs
+
+
+@pytest.mark.parametrize("sched", [
+    dict(persistent=0, snake=0, use_graph=0),
+    dict(persistent=0, snake=1, use_graph=1),
+    dict(persistent=1, snake=1, use_graph=0),
+    dict(persistent=1, snake=0, use_graph=1),
+])
+def test_batch_equals_single_pairs(sched):
+    params, frames = _batch_inputs()
+    want = _single(params, frames)
+    b = bm.Batch(params)
+    b.set_schedule(**sched)
+    b.load_frames(b.pack_frames(frames))
+    for _ in range(2):  # a replayed step gives the same result
+        b.run()
+        b.synchronize()
+        got = b.read_flows()
+        for k, ((gu, gv), (wu, wv)) in enumerate(zip(got, want)):
+            assert np.array_equal(gu, wu) and np.array_equal(gv, wv), (sched, k)
+    b.close()
+
+
+def test_batch_n128_and_unfiltered():
+    params = [bm.BMParams.derive(w, h, 1.5, 1.5, N=128, filter=0) for w, h in SIZES[:3]]
+    frames = [synth.make_pair(40 + k, w, h, 4.0)[:2] for k, (w, h) in enumerate(SIZES[:3])]
+    want = _single(params, frames)
+    b = bm.Batch(params)
+    b.set_schedule(persistent=1, use_graph=1)
+    b.load_frames(b.pack_frames(frames))
+    b.run()
+    b.synchronize()
+    for (gu, gv), (wu, wv) in zip(b.read_flows(), want):
+        assert np.array_equal(gu, wu) and np.array_equal(gv, wv)
+    b.close()
+
+
+def test_autotune_and_cache(tmp_path):
+    params, frames = _batch_inputs()
+    b = bm.Batch(params)
+    b.load_frames(b.pack_frames(frames))
+    cache = str(tmp_path / "tune.jsonl")
+    rep = b.autotune(cache, reps=2)
+    assert "persistent=" in rep
+    line = json.loads(open(cache).read().strip().splitlines()[-1])
+    assert {"key", "persistent", "blocks_per_sm", "snake", "use_graph", "ms"} <= set(line)
+    chosen = b.schedule()
+    b.close()
+    b2 = bm.Batch(params)
+    rep2 = b2.autotune(cache)
+    assert rep2.startswith("cached")
+    assert b2.schedule()["persistent"] == chosen["persistent"]
+    b2.load_frames(b2.pack_frames(frames))
+    b2.run()
+    b2.synchronize()
+    want = _single(params, frames)
+    for (gu, gv), (wu, wv) in zip(b2.read_flows(), want):
+        assert np.array_equal(gu, wu) and np.array_equal(gv, wv)
+    b2.close()
+
+
+def test_grid_barrier_gives_up():
+    st, timed_out = bm.selftest_barrier(2, 2, 100000)
+    assert st == bm.BM_OK and timed_out == 0
+    st, timed_out = bm.selftest_barrier(2, 3, 2000)  # nobody can pass: all blocks give up
+    assert st == bm.BM_ERR_TIMEOUT and timed_out == 1
+    # the context stays usable
+    x = torch.ones(4, device="cuda")
+    assert float(x.sum()) == 4.0
