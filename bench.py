@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-pairs", type=int, default=2, help="pairs in the CPU-baseline sample")
+    ap.add_argument("--no-batched", action="store_true", help="skip the 64-pair batched workload")
+    ap.add_argument("--batch-pairs", type=int, default=64)
     return ap.parse_args()
 
 
@@ -193,6 +195,7 @@ def run_engine(args, torch, world, rank):
     import briefmatch_gb300 as bm
 
     frames, flows = make_workload(rank)
+    batch_inputs = None if args.no_batched else make_batch_workload(args.batch_pairs)
     prm = bm.BMParams.derive(W, H, UP, UP, N=NBITS)
     eng = bm.BriefMatch(prm)
     eng.setup()
@@ -298,6 +301,12 @@ def run_engine(args, torch, world, rank):
     kernels = {k: {"launches": c, "ms": round(t, 4), "share": round(t / total_k, 4)} for k, (c, t) in
                sorted(kstats.items(), key=lambda kv: -kv[1][1])}
 
+    batched = None
+    if batch_inputs is not None:
+        eng_stream_restore = stream.cuda_stream
+        batched = run_batched(args, torch, *batch_inputs)
+        eng.set_stream(eng_stream_restore)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(prm, pattern, frames, args.cpu_pairs)
@@ -318,10 +327,110 @@ def run_engine(args, torch, world, rank):
         "roofline": roofline,
         "kernels": kernels,
         "cpu_baseline": cpu,
+        "batched": batched,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
     eng.clean()
+
+
+BATCH_SEED = 20261204
+
+
+def _make_batch_pair(args):
+    k, w, h = args
+    from briefmatch_gb300 import synth
+
+    f0, f1, u, v = synth.make_pair(BATCH_SEED + k, w, h, vmax=15.0)
+    return f0, f1, u, v
+
+
+def make_batch_workload(pairs):
+    """64 pairs of uneven size (widths U[320,1920], heights U[240,1080], multiples of
+    4), generated in a spawn-started process pool (before any GPU work)."""
+    import multiprocessing as mp
+
+    from briefmatch_gb300 import synth
+
+    sizes = synth.make_batch_sizes(BATCH_SEED, count=pairs)
+    jobs = [(k, w, h) for k, (w, h) in enumerate(sizes)]
+    with mp.get_context("spawn").Pool(min(16, os.cpu_count() or 1)) as pool:
+        data = pool.map(_make_batch_pair, jobs)
+    return sizes, data
+
+
+def run_batched(args, torch, sizes, data):
+    """The batched workload: all pairs through one autotuned batch step (persistent
+    matching launch and/or per-level launches, replayed as a CUDA graph) against the
+    same pairs run one after another through per-pair contexts (plain launches)."""
+    import numpy as np
+
+    import briefmatch_gb300 as bm
+
+    params = [bm.BMParams.derive(w, h, UP, UP, N=NBITS) for w, h in sizes]
+    out_px = sum(w * h for w, h in sizes)
+    stream = torch.cuda.current_stream()
+    b = bm.Batch(params)
+    b.set_stream(stream.cuda_stream)
+    packed = b.pack_frames([(d[0], d[1]) for d in data])
+    d_packed = torch.from_numpy(packed).cuda()
+    b.load_frames(d_packed.data_ptr(), on_device=True)
+    report = b.autotune(None, reps=2)
+    for _ in range(args.warmup):
+        b.run()
+    b.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    launches0 = b.launch_count()
+    for s0, s1 in ev:
+        s0.record(stream)
+        b.run()
+        s1.record(stream)
+    b.synchronize()
+    batch_ms = sum(s0.elapsed_time(s1) for s0, s1 in ev) / args.steps
+    flows = b.read_flows()
+    epe = float(np.mean([np.mean(np.hypot(f[0] - d[2], f[1] - d[3])) for f, d in zip(flows, data)]))
+    sched = b.schedule()
+    b.close()
+    del d_packed
+
+    # the same pairs, one after another, each through its own plain context
+    engines = []
+    d_frames = []
+    for p, d in zip(params, data):
+        e = bm.BriefMatch(p)
+        e.setup()
+        e.set_stream(stream.cuda_stream)
+        engines.append(e)
+        d_frames.append((torch.from_numpy(d[0]).cuda(), torch.from_numpy(d[1]).cuda()))
+
+    def seq_step():
+        for e, (f0, f1) in zip(engines, d_frames):
+            e.reset_sequence()
+            e.set_rng_position(0)
+            e.frame(f0.data_ptr(), True)
+            e.frame(f1.data_ptr(), True)
+
+    for _ in range(args.warmup):
+        seq_step()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for s0, s1 in ev:
+        s0.record(stream)
+        seq_step()
+        s1.record(stream)
+    torch.cuda.synchronize()
+    seq_ms = sum(s0.elapsed_time(s1) for s0, s1 in ev) / args.steps
+    for e in engines:
+        e.clean()
+    return {
+        "workload": "%d pairs, widths U[320,1920] x heights U[240,1080] (multiples of 4), u2.9, N128, one pair "
+                    "(2 frames) each" % len(sizes),
+        "output_mpx_per_step": out_px / 1e6,
+        "value": out_px / (batch_ms * 1e-3) / 1e6, "unit": UNIT, "ms_per_step": batch_ms,
+        "sequential_value": out_px / (seq_ms * 1e-3) / 1e6, "sequential_ms_per_step": seq_ms,
+        "speedup_vs_sequential": seq_ms / batch_ms,
+        "schedule": sched, "autotune": report, "epe_mean": epe,
+    }
 
 
 def cpu_baseline(prm, pattern, frames, pairs):

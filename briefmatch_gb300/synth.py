@@ -18,6 +18,12 @@ import numpy as np
 
 
 def _gauss_blur(img, sigma):
+    try:
+        from scipy.ndimage import gaussian_filter
+
+        return gaussian_filter(img, sigma, mode="reflect", truncate=3.0)
+    except ImportError:
+        pass
     r = int(np.ceil(3 * sigma))
     t = np.arange(-r, r + 1, dtype=np.float64)
     k = np.exp(-t * t / (2 * sigma * sigma))
@@ -74,6 +80,13 @@ def make_flow(rng, w, h, vmax=10.0):
 
 
 def _bilinear(img, x, y):
+    try:
+        from scipy.ndimage import map_coordinates
+
+        return map_coordinates(img, [np.clip(y, 0, img.shape[0] - 1), np.clip(x, 0, img.shape[1] - 1)], order=1,
+                               mode="nearest")
+    except ImportError:
+        pass
     h, w = img.shape
     x = np.clip(x, 0, w - 1)
     y = np.clip(y, 0, h - 1)
