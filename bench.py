@@ -201,8 +201,11 @@ def run_engine(args, torch, world, rank):
     eng.setup()
     pattern = prm.make_pattern(SEED)
     eng.set_pattern(pattern)
-    stream = torch.cuda.current_stream()
+    # one explicit (non-default) stream carries the engine's work, the L2 flush and
+    # the timing events
+    stream = torch.cuda.Stream()
     eng.set_stream(stream.cuda_stream)
+    torch.cuda.set_stream(stream)
 
     d_frames = torch.from_numpy(np.stack(frames)).cuda()
     d_u = torch.empty(PAIRS, H, W, device="cuda")
@@ -303,9 +306,7 @@ def run_engine(args, torch, world, rank):
 
     batched = None
     if batch_inputs is not None:
-        eng_stream_restore = stream.cuda_stream
         batched = run_batched(args, torch, *batch_inputs)
-        eng.set_stream(eng_stream_restore)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
