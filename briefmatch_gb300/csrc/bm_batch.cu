@@ -59,12 +59,13 @@ struct PairDev {
     const unsigned int* nny;
 };
 
+// The pairs [lo, hi) (internal order) that one launch covers: a "wave".
 struct BatchDev {
     const PairDev* pairs;
     const unsigned int* pre_up;   // [count+1] exclusive prefix of up-sampled-grid tiles
     const unsigned int* pre_in;   // input-resolution 32x8 tiles
     const unsigned int* pre_tri;  // trilateral 32x16 tiles
-    int count;
+    int lo, hi;
     int N;
 };
 
@@ -112,9 +113,10 @@ __device__ __forceinline__ bool grid_sync(GridSync* gs, unsigned int nblocks, un
     return ok != 0;
 }
 
-__device__ __forceinline__ int find_pair(const unsigned int* __restrict__ pre, int count, unsigned int tile)
+// Pair of the wave [wlo, whi) that owns tile `tile` (a global tile index).
+__device__ __forceinline__ int find_pair(const unsigned int* __restrict__ pre, int wlo, int whi, unsigned int tile)
 {
-    int lo = 0, hi = count - 1;
+    int lo = wlo, hi = whi - 1;
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
         if (__ldg(pre + mid) <= tile)
@@ -130,8 +132,8 @@ __device__ __forceinline__ int find_pair(const unsigned int* __restrict__ pre, i
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_b_guide(BatchDev bd)
 {
-    const unsigned int tile = blockIdx.x;
-    const int i = find_pair(bd.pre_in, bd.count, tile);
+    const unsigned int tile = bd.pre_in[bd.lo] + blockIdx.x;
+    const int i = find_pair(bd.pre_in, bd.lo, bd.hi, tile);
     const PairDev& P = bd.pairs[i];
     const unsigned int t = tile - bd.pre_in[i];
     const int x = (int)(t % P.first_in_tile_x) * TX + threadIdx.x, y = (int)(t / P.first_in_tile_x) * TY + threadIdx.y;
@@ -142,8 +144,8 @@ __global__ void __launch_bounds__(256) k_b_guide(BatchDev bd)
 
 __global__ void __launch_bounds__(256) k_b_upsample(BatchDev bd, int which)
 {
-    const unsigned int tile = blockIdx.x;
-    const int i = find_pair(bd.pre_up, bd.count, tile);
+    const unsigned int tile = bd.pre_up[bd.lo] + blockIdx.x;
+    const int i = find_pair(bd.pre_up, bd.lo, bd.hi, tile);
     const PairDev& P = bd.pairs[i];
     const unsigned int t = tile - bd.pre_up[i];
     const int x = (int)(t % P.first_up_tile_x) * TX + threadIdx.x, y = (int)(t / P.first_up_tile_x) * TY + threadIdx.y;
@@ -159,8 +161,8 @@ __global__ void __launch_bounds__(256) k_b_features(BatchDev bd, int which)
 {
     __shared__ int4 s_pat[BM_PATCH_MAX / 4];
     __shared__ int2 s_off[BM_PATCH_MAX / 4];
-    const unsigned int tile = blockIdx.x;
-    const int i = find_pair(bd.pre_up, bd.count, tile);
+    const unsigned int tile = bd.pre_up[bd.lo] + blockIdx.x;
+    const int i = find_pair(bd.pre_up, bd.lo, bd.hi, tile);
     const PairDev& P = bd.pairs[i];
     const unsigned int t = tile - bd.pre_up[i];
     const int bx = (int)(t % P.first_up_tile_x) * TX, by = (int)(t / P.first_up_tile_x) * TY;
@@ -181,7 +183,7 @@ __global__ void __launch_bounds__(256) k_b_features(BatchDev bd, int which)
 // Tile `tile` of the up-sampled grids, visited in reverse order when rev is set.
 __device__ __forceinline__ bool up_tile(const BatchDev& bd, unsigned int tile, int& i, int& x, int& y)
 {
-    i = find_pair(bd.pre_up, bd.count, tile);
+    i = find_pair(bd.pre_up, bd.lo, bd.hi, tile);
     const PairDev& P = bd.pairs[i];
     const unsigned int t = tile - bd.pre_up[i];
     x = (int)(t % P.first_up_tile_x) * TX + threadIdx.x;
@@ -192,8 +194,8 @@ __device__ __forceinline__ bool up_tile(const BatchDev& bd, unsigned int tile, i
 template <int NSP>
 __global__ void __launch_bounds__(256) k_b_initialize(BatchDev bd, int cur, int rev)
 {
-    const unsigned int total = bd.pre_up[bd.count];
-    const unsigned int tile = rev ? total - 1 - blockIdx.x : blockIdx.x;
+    const unsigned int base = bd.pre_up[bd.lo], total = bd.pre_up[bd.hi] - base;
+    const unsigned int tile = base + (rev ? total - 1 - blockIdx.x : blockIdx.x);
     int i, x, y;
     if (!up_tile(bd, tile, i, x, y)) return;
     const PairDev& P = bd.pairs[i];
@@ -203,8 +205,8 @@ __global__ void __launch_bounds__(256) k_b_initialize(BatchDev bd, int cur, int 
 template <int NSP, bool RS>
 __global__ void __launch_bounds__(256) k_b_jump(BatchDev bd, int cur, int p, int pd, int doubleProp, RsArgs rs, int rev)
 {
-    const unsigned int total = bd.pre_up[bd.count];
-    const unsigned int tile = rev ? total - 1 - blockIdx.x : blockIdx.x;
+    const unsigned int base = bd.pre_up[bd.lo], total = bd.pre_up[bd.hi] - base;
+    const unsigned int tile = base + (rev ? total - 1 - blockIdx.x : blockIdx.x);
     int i, x, y;
     if (!up_tile(bd, tile, i, x, y)) return;
     const PairDev& P = bd.pairs[i];
@@ -226,12 +228,12 @@ struct MatchPlan {
 template <int NSP>
 __global__ void __launch_bounds__(256) k_b_match_persistent(BatchDev bd, MatchPlan plan, GridSync* gs)
 {
-    const unsigned int total = bd.pre_up[bd.count];
+    const unsigned int base = bd.pre_up[bd.lo], total = bd.pre_up[bd.hi] - base;
     int cur = 0;
     unsigned int phase = 0;
-    for (unsigned int tile = blockIdx.x; tile < total; tile += gridDim.x) {
+    for (unsigned int k = blockIdx.x; k < total; k += gridDim.x) {
         int i, x, y;
-        if (up_tile(bd, tile, i, x, y)) {
+        if (up_tile(bd, base + k, i, x, y)) {
             const PairDev& P = bd.pairs[i];
             init_px<NSP>(P.F[0], P.F[1], P.flow[0], P.flow[1], P.cost, P.sx, P.sy, 1, x, y);
         }
@@ -252,7 +254,7 @@ __global__ void __launch_bounds__(256) k_b_match_persistent(BatchDev bd, MatchPl
             rs.seed = plan.seed;
             rs.call = (unsigned long long)it;
             for (unsigned int k = blockIdx.x; k < total; k += gridDim.x) {
-                const unsigned int tile = rev ? total - 1 - k : k;
+                const unsigned int tile = base + (rev ? total - 1 - k : k);
                 int i, x, y;
                 if (!up_tile(bd, tile, i, x, y)) continue;
                 const PairDev& P = bd.pairs[i];
@@ -273,8 +275,8 @@ __global__ void __launch_bounds__(256) k_b_match_persistent(BatchDev bd, MatchPl
 
 __global__ void __launch_bounds__(256) k_b_downsample(BatchDev bd, int cur)
 {
-    const unsigned int tile = blockIdx.x;
-    const int i = find_pair(bd.pre_in, bd.count, tile);
+    const unsigned int tile = bd.pre_in[bd.lo] + blockIdx.x;
+    const int i = find_pair(bd.pre_in, bd.lo, bd.hi, tile);
     const PairDev& P = bd.pairs[i];
     const unsigned int t = tile - bd.pre_in[i];
     const int x = (int)(t % P.first_in_tile_x) * TX + threadIdx.x, y = (int)(t / P.first_in_tile_x) * TY + threadIdx.y;
@@ -293,8 +295,8 @@ __global__ void __launch_bounds__(256) k_b_downsample(BatchDev bd, int cur)
 template <int FS>
 __global__ void __launch_bounds__(256) k_b_median(BatchDev bd, int dir)
 {
-    const unsigned int tile = blockIdx.x;
-    const int i = find_pair(bd.pre_in, bd.count, tile);
+    const unsigned int tile = bd.pre_in[bd.lo] + blockIdx.x;
+    const int i = find_pair(bd.pre_in, bd.lo, bd.hi, tile);
     const PairDev& P = bd.pairs[i];
     const unsigned int t = tile - bd.pre_in[i];
     const int x = (int)(t % P.first_in_tile_x) * TX + threadIdx.x, y = (int)(t / P.first_in_tile_x) * TY + threadIdx.y;
@@ -309,8 +311,8 @@ __global__ void __launch_bounds__(256) k_b_median(BatchDev bd, int dir)
 __global__ void __launch_bounds__(TX * TRI_TY) k_b_trilateral(BatchDev bd, int filter)
 {
     extern __shared__ float4 smem4[];
-    const unsigned int tile = blockIdx.x;
-    const int i = find_pair(bd.pre_tri, bd.count, tile);
+    const unsigned int tile = bd.pre_tri[bd.lo] + blockIdx.x;
+    const int i = find_pair(bd.pre_tri, bd.lo, bd.hi, tile);
     const PairDev& P = bd.pairs[i];
     const unsigned int t = tile - bd.pre_tri[i];
     const int bx0 = (int)(t % P.first_tri_tile_x) * TX, by0 = (int)(t / P.first_tri_tile_x) * TRI_BY;
@@ -357,6 +359,9 @@ struct bm_batch {
     size_t frames_offset = 0, frames_bytes = 0;   // packed input frames inside the arena
     size_t flows_offset = 0, flows_bytes = 0;     // packed refined flows (U,V per pair)
     std::vector<size_t> frame_off, flow_off;
+    std::vector<uint32_t> order;   // internal index -> caller's pair index (ascending working set)
+    std::vector<uint32_t> pos;     // caller's pair index -> internal index
+    std::vector<size_t> ws;        // working set of each pair (internal order), bytes
     int max_fsize = 1, max_tri_s = 0;
     size_t tri_smem = 0;
     int coop_blocks_per_sm = 0, num_sms = 0;
@@ -386,16 +391,41 @@ bm_status bfail(bm_status st, const char* fmt, ...)
         if (e_ != cudaSuccess) return bfail(BM_ERR_CUDA, "%s (%s:%d)", cudaGetErrorString(e_), __FILE__, __LINE__); \
     } while (0)
 
-BatchDev batch_dev(const bm_batch* b)
+BatchDev batch_dev(const bm_batch* b, int lo, int hi)
 {
     BatchDev bd;
     bd.pairs = b->d_pairs;
     bd.pre_up = b->d_pre;
     bd.pre_in = b->d_pre + (b->count + 1);
     bd.pre_tri = b->d_pre + 2 * (b->count + 1);
-    bd.count = (int)b->count;
+    bd.lo = lo;
+    bd.hi = hi;
     bd.N = (int)b->N;
     return bd;
+}
+
+// Consecutive runs of pairs (internal order: ascending working set) whose working
+// sets add up to at most `budget` bytes; a pair larger than the budget is a wave of
+// its own.  budget 0: one wave.
+std::vector<std::pair<int, int>> make_waves(const bm_batch* b, uint64_t budget)
+{
+    std::vector<std::pair<int, int>> w;
+    if (budget == 0) {
+        w.push_back({0, (int)b->count});
+        return w;
+    }
+    int lo = 0;
+    uint64_t acc = 0;
+    for (int j = 0; j < (int)b->count; j++) {
+        if (j > lo && acc + b->ws[j] > budget) {
+            w.push_back({lo, j});
+            lo = j;
+            acc = 0;
+        }
+        acc += b->ws[j];
+    }
+    w.push_back({lo, (int)b->count});
+    return w;
 }
 
 #define BB_NSP(nsp, ...)                                            \
@@ -408,11 +438,24 @@ BatchDev batch_dev(const bm_batch* b)
     default: return bfail(BM_ERR_INVALID, "bad descriptor stride"); \
     }
 
-// Enqueue one batch step on b->stream (no synchronisation).
+bm_status enqueue_wave(bm_batch* b, const bm_batch_schedule& s, int lo, int hi);
+
+// Enqueue one batch step on b->stream (no synchronisation): every wave runs the
+// whole pipeline before the next starts.
 bm_status enqueue_step(bm_batch* b, const bm_batch_schedule& s)
 {
-    const BatchDev bd = batch_dev(b);
-    const unsigned int t_up = b->pre_up[b->count], t_in = b->pre_in[b->count], t_tri = b->pre_tri[b->count];
+    for (const auto& w : make_waves(b, s.wave_bytes)) {
+        bm_status st = enqueue_wave(b, s, w.first, w.second);
+        if (st != BM_OK) return st;
+    }
+    return BM_OK;
+}
+
+bm_status enqueue_wave(bm_batch* b, const bm_batch_schedule& s, int lo, int hi)
+{
+    const BatchDev bd = batch_dev(b, lo, hi);
+    const unsigned int t_up = b->pre_up[hi] - b->pre_up[lo], t_in = b->pre_in[hi] - b->pre_in[lo],
+                       t_tri = b->pre_tri[hi] - b->pre_tri[lo];
     cudaStream_t st = b->stream;
     const dim3 blk(TX, TY);
     k_b_guide<<<t_in, blk, 0, st>>>(bd);
@@ -603,6 +646,23 @@ bm_status bm_batch_create(const bm_params* pairs, uint32_t count, bm_batch** out
     b->sched.snake = 1;
     b->sched.use_graph = 1;
     b->sched.spin_limit = 1ull << 24;
+    b->sched.wave_bytes = 0;
+    {
+        std::vector<size_t> ws_api(count);
+        for (uint32_t i = 0; i < count; i++) {
+            const size_t n = (size_t)pairs[i].sx * pairs[i].sy, ni = (size_t)pairs[i].sx_in * pairs[i].sy_in;
+            ws_api[i] = n * (8 * (size_t)b->nsp + 14) + ni * 38;
+        }
+        b->order.resize(count);
+        for (uint32_t i = 0; i < count; i++) b->order[i] = i;
+        std::stable_sort(b->order.begin(), b->order.end(), [&](uint32_t a, uint32_t c) { return ws_api[a] < ws_api[c]; });
+        b->pos.resize(count);
+        b->ws.resize(count);
+        for (uint32_t j = 0; j < count; j++) {
+            b->pos[b->order[j]] = j;
+            b->ws[j] = ws_api[b->order[j]];
+        }
+    }
 
     // layout
     struct Off {
@@ -685,10 +745,11 @@ bm_status bm_batch_create(const bm_params* pairs, uint32_t count, bm_batch** out
     b->pre_in.assign(count + 1, 0);
     b->pre_tri.assign(count + 1, 0);
     std::vector<float> pattern(4 * (size_t)b->N);
-    for (uint32_t i = 0; i < count; i++) {
+    for (uint32_t j = 0; j < count; j++) {
+        const uint32_t i = b->order[j];  // caller's index of internal pair j
         const bm_params& p = pairs[i];
         const Off& o = offs[i];
-        PairDev& d = b->pairs[i];
+        PairDev& d = b->pairs[j];
         d.sx = (int)p.sx;
         d.sy = (int)p.sy;
         d.sx_in = (int)p.sx_in;
@@ -709,9 +770,9 @@ bm_status bm_batch_create(const bm_params* pairs, uint32_t count, bm_batch** out
         d.first_up_tile_x = (d.sx + TX - 1) / TX;
         d.first_in_tile_x = (d.sx_in + TX - 1) / TX;
         d.first_tri_tile_x = (d.sx_in + TX - 1) / TX;
-        b->pre_up[i + 1] = b->pre_up[i] + (unsigned)(d.first_up_tile_x * ((d.sy + TY - 1) / TY));
-        b->pre_in[i + 1] = b->pre_in[i] + (unsigned)(d.first_in_tile_x * ((d.sy_in + TY - 1) / TY));
-        b->pre_tri[i + 1] = b->pre_tri[i] + (unsigned)(d.first_tri_tile_x * ((d.sy_in + TRI_BY - 1) / TRI_BY));
+        b->pre_up[j + 1] = b->pre_up[j] + (unsigned)(d.first_up_tile_x * ((d.sy + TY - 1) / TY));
+        b->pre_in[j + 1] = b->pre_in[j] + (unsigned)(d.first_in_tile_x * ((d.sy_in + TY - 1) / TY));
+        b->pre_tri[j + 1] = b->pre_tri[j] + (unsigned)(d.first_tri_tile_x * ((d.sy_in + TRI_BY - 1) / TRI_BY));
         char* A = b->arena;
         d.frame[0] = reinterpret_cast<const uint8_t*>(A + b->frames_offset + b->frame_off[2 * i]);
         d.frame[1] = reinterpret_cast<const uint8_t*>(A + b->frames_offset + b->frame_off[2 * i + 1]);
@@ -821,7 +882,7 @@ bm_status bm_batch_set_pattern(bm_batch* b, uint32_t pair, const float* h_patter
     std::vector<int4> pat(b->N);
     std::vector<int2> off(BM_PATCH_MAX / 4, make_int2(0, 0));
     int rmax = 0;
-    const int sx = b->pairs[pair].sx;
+    const int sx = b->pairs[b->pos[pair]].sx;
     for (uint32_t s = 0; s < b->N; s++) {
         int v[4];
         for (int k = 0; k < 4; k++) {
@@ -831,12 +892,13 @@ bm_status bm_batch_set_pattern(bm_batch* b, uint32_t pair, const float* h_patter
         pat[s] = make_int4(v[0], v[1], v[2], v[3]);
         off[s] = make_int2(v[0] + v[1] * sx, v[2] + v[3] * sx);
     }
-    PairDev& d = b->pairs[pair];
+    const uint32_t j = b->pos[pair];
+    PairDev& d = b->pairs[j];
     d.rmax = rmax;
     BB_CUDA(cudaMemcpyAsync((void*)d.pat, pat.data(), b->N * sizeof(int4), cudaMemcpyHostToDevice, b->stream));
     BB_CUDA(cudaMemcpyAsync((void*)d.off, off.data(), off.size() * sizeof(int2), cudaMemcpyHostToDevice, b->stream));
     if (b->d_pairs)
-        BB_CUDA(cudaMemcpyAsync(b->d_pairs + pair, &d, sizeof(PairDev), cudaMemcpyHostToDevice, b->stream));
+        BB_CUDA(cudaMemcpyAsync(b->d_pairs + j, &d, sizeof(PairDev), cudaMemcpyHostToDevice, b->stream));
     BB_CUDA(cudaStreamSynchronize(b->stream));
     return BM_OK;
 }
@@ -875,9 +937,10 @@ bm_status bm_batch_read_flows(bm_batch* b, float* packed, size_t bytes, int on_d
 bm_status bm_batch_flow_ptr(bm_batch* b, uint32_t pair, float** d_u, float** d_v)
 {
     if (!b || pair >= b->count || !d_u || !d_v) return bfail(BM_ERR_INVALID, "bm_batch_flow_ptr: bad argument");
-    const size_t ni = (size_t)b->pairs[pair].sx_in * b->pairs[pair].sy_in;
-    *d_u = b->pairs[pair].flow_out;
-    *d_v = b->pairs[pair].flow_out + ni;
+    const PairDev& d = b->pairs[b->pos[pair]];
+    const size_t ni = (size_t)d.sx_in * d.sy_in;
+    *d_u = d.flow_out;
+    *d_v = d.flow_out + ni;
     return BM_OK;
 }
 
@@ -950,6 +1013,7 @@ bm_status bm_batch_autotune(bm_batch* b, const char* cache_path, int reps, char*
             ok &= grab("blocks_per_sm", v) && ((s.blocks_per_sm = (uint32_t)v), true);
             ok &= grab("snake", v) && ((s.snake = (uint32_t)v), true);
             ok &= grab("use_graph", v) && ((s.use_graph = (uint32_t)v), true);
+            ok &= grab("wave_bytes", v) && ((s.wave_bytes = v), true);
             if (ok) {
                 bm_batch_set_schedule(b, &s);
                 if (report) std::snprintf(report, report_len, "cached: %s", hit.c_str());
@@ -958,20 +1022,18 @@ bm_status bm_batch_autotune(bm_batch* b, const char* cache_path, int reps, char*
         }
     }
     std::vector<bm_batch_schedule> cands;
-    for (uint32_t snake = 0; snake <= 1; snake++) {
-        bm_batch_schedule s = b->sched;
-        s.persistent = 0;
-        s.snake = snake;
-        s.use_graph = 1;
-        cands.push_back(s);
-    }
-    for (int bps : {b->coop_blocks_per_sm, std::max(1, b->coop_blocks_per_sm / 2)}) {
-        bm_batch_schedule s = b->sched;
-        s.persistent = 1;
-        s.blocks_per_sm = (uint32_t)bps;
-        s.snake = 1;
-        s.use_graph = 1;
-        cands.push_back(s);
+    const uint64_t MB = 1ull << 20;
+    const uint64_t waves[4] = {0ull, 64 * MB, 96 * MB, 160 * MB};
+    for (uint64_t wave : waves) {
+        for (uint32_t persistent = 0; persistent <= 1; persistent++) {
+            bm_batch_schedule s = b->sched;
+            s.persistent = persistent;
+            s.blocks_per_sm = (uint32_t)b->coop_blocks_per_sm;
+            s.snake = 1;
+            s.use_graph = 1;
+            s.wave_bytes = wave;
+            cands.push_back(s);
+        }
     }
     if (reps < 1) reps = 3;
     double best_ms = 1e30;
@@ -985,8 +1047,7 @@ bm_status bm_batch_autotune(bm_batch* b, const char* cache_path, int reps, char*
         bm_status st = bm_batch_run(b);
         if (st == BM_OK) st = bm_batch_synchronize(b);
         if (st != BM_OK) {
-            rep << "{persistent=" << s.persistent << ",bps=" << s.blocks_per_sm << ",snake=" << s.snake
-                << ": failed} ";
+            rep << "{persistent=" << s.persistent << ",wave=" << (s.wave_bytes >> 20) << "MB: failed} ";
             continue;
         }
         cudaEventRecord(e0, b->stream);
@@ -996,7 +1057,7 @@ bm_status bm_batch_autotune(bm_batch* b, const char* cache_path, int reps, char*
         float ms = 0;
         cudaEventElapsedTime(&ms, e0, e1);
         ms /= reps;
-        rep << "{persistent=" << s.persistent << ",bps=" << s.blocks_per_sm << ",snake=" << s.snake << ": "
+        rep << "{persistent=" << s.persistent << ",wave=" << (s.wave_bytes >> 20) << "MB: "
             << (st == BM_OK ? std::to_string(ms) : std::string("failed")) << " ms} ";
         if (st == BM_OK && ms < best_ms) {
             best_ms = ms;
@@ -1010,10 +1071,11 @@ bm_status bm_batch_autotune(bm_batch* b, const char* cache_path, int reps, char*
         std::ofstream out(cache_path, std::ios::app);
         out << "{\"key\": \"" << key << "\", \"persistent\": " << best.persistent << ", \"blocks_per_sm\": "
             << best.blocks_per_sm << ", \"snake\": " << best.snake << ", \"use_graph\": " << best.use_graph
-            << ", \"ms\": " << best_ms << "}\n";
+            << ", \"wave_bytes\": " << best.wave_bytes << ", \"ms\": " << best_ms << "}\n";
     }
-    if (report) std::snprintf(report, report_len, "%s-> persistent=%u bps=%u snake=%u", rep.str().c_str(),
-                              best.persistent, best.blocks_per_sm, best.snake);
+    if (report)
+        std::snprintf(report, report_len, "%s-> persistent=%u wave=%lluMB", rep.str().c_str(), best.persistent,
+                      (unsigned long long)(best.wave_bytes >> 20));
     return BM_OK;
 }
 

@@ -211,6 +211,8 @@ typedef struct bm_batch_schedule {
     uint32_t snake;          /* alternate the tile order between passes */
     uint32_t use_graph;      /* capture the step in a CUDA graph and replay it */
     uint64_t spin_limit;     /* polls before a grid barrier gives up (BM_ERR_TIMEOUT) */
+    uint64_t wave_bytes;     /* run pairs in waves whose working sets sum to at most this
+                                (smallest pairs first, so a wave stays L2-resident); 0 = one wave */
 } bm_batch_schedule;
 
 bm_status bm_batch_create(const bm_params* pairs, uint32_t count, bm_batch** out);

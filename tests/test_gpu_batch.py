@@ -41,6 +41,8 @@ def _single(params, frames):
     dict(persistent=0, snake=1, use_graph=1),
     dict(persistent=1, snake=1, use_graph=0),
     dict(persistent=1, snake=0, use_graph=1),
+    dict(persistent=0, snake=1, use_graph=1, wave_bytes=1),          # one pair per wave
+    dict(persistent=1, snake=1, use_graph=1, wave_bytes=3 << 20),    # small waves
 ])
 def test_batch_equals_single_pairs(sched):
     params, frames = _batch_inputs()
