@@ -156,30 +156,6 @@ __global__ void __launch_bounds__(256) k_b_upsample(BatchDev bd, int which)
         upsample_px<uint8_t>(P.frame[which], P.up, P.sx_in, P.sy_in, P.sx, P.lx, P.ix, P.ly, P.iy, x, y);
 }
 
-template <int NSP>
-__global__ void __launch_bounds__(256) k_b_features(BatchDev bd, int which)
-{
-    __shared__ int4 s_pat[BM_PATCH_MAX / 4];
-    __shared__ int2 s_off[BM_PATCH_MAX / 4];
-    const unsigned int tile = bd.pre_up[bd.lo] + blockIdx.x;
-    const int i = find_pair(bd.pre_up, bd.lo, bd.hi, tile);
-    const PairDev& P = bd.pairs[i];
-    const unsigned int t = tile - bd.pre_up[i];
-    const int bx = (int)(t % P.first_up_tile_x) * TX, by = (int)(t / P.first_up_tile_x) * TY;
-    const int tid = threadIdx.y * TX + threadIdx.x;
-    for (int k = tid; k < NSP * 32; k += TX * TY) {
-        s_off[k] = __ldg(P.off + k);
-        if (k < bd.N) s_pat[k] = __ldg(P.pat + k);
-    }
-    __syncthreads();
-    const int x = bx + threadIdx.x, y = by + threadIdx.y;
-    if (x >= P.sx || y >= P.sy) return;
-    if (tile_interior(bx, by, P.sx, P.sy, P.rmax))
-        features_interior_px<NSP>(P.up, P.F[which], P.sx, x, y, s_off);
-    else
-        features_border_px<NSP>(P.up, P.F[which], P.sx, P.sy, bd.N, s_pat, x, y);
-}
-
 // Tile `tile` of the up-sampled grids, visited in reverse order when rev is set.
 __device__ __forceinline__ bool up_tile(const BatchDev& bd, unsigned int tile, int& i, int& x, int& y)
 {
@@ -292,46 +268,6 @@ __global__ void __launch_bounds__(256) k_b_downsample(BatchDev bd, int cur)
                   x, y);
 }
 
-template <int FS>
-__global__ void __launch_bounds__(256) k_b_median(BatchDev bd, int dir)
-{
-    const unsigned int tile = bd.pre_in[bd.lo] + blockIdx.x;
-    const int i = find_pair(bd.pre_in, bd.lo, bd.hi, tile);
-    const PairDev& P = bd.pairs[i];
-    const unsigned int t = tile - bd.pre_in[i];
-    const int x = (int)(t % P.first_in_tile_x) * TX + threadIdx.x, y = (int)(t / P.first_in_tile_x) * TY + threadIdx.y;
-    if (x >= P.sx_in || y >= P.sy_in) return;
-    const size_t ni = (size_t)P.sx_in * P.sy_in;
-    const float* in = dir ? P.flow_in : P.tmp;
-    float* out = dir ? P.tmp : P.flow_med;
-    const int fs = P.fsize == 0 ? 1 : P.fsize;
-    median_px<FS>(in + blockIdx.y * ni, out + blockIdx.y * ni, dir, fs, P.sx_in, P.sy_in, x, y);
-}
-
-__global__ void __launch_bounds__(TX * TRI_TY) k_b_trilateral(BatchDev bd, int filter)
-{
-    extern __shared__ float4 smem4[];
-    const unsigned int tile = bd.pre_tri[bd.lo] + blockIdx.x;
-    const int i = find_pair(bd.pre_tri, bd.lo, bd.hi, tile);
-    const PairDev& P = bd.pairs[i];
-    const unsigned int t = tile - bd.pre_tri[i];
-    const int bx0 = (int)(t % P.first_tri_tile_x) * TX, by0 = (int)(t / P.first_tri_tile_x) * TRI_BY;
-    const size_t ni = (size_t)P.sx_in * P.sy_in;
-    if (!filter) {
-        for (int r = threadIdx.y; r < TRI_BY; r += TRI_TY) {
-            const int x = bx0 + threadIdx.x, y = by0 + r;
-            if (x < P.sx_in && y < P.sy_in) {
-                const size_t o = (size_t)y * P.sx_in + x;
-                P.flow_out[o] = P.flow_in[o];
-                P.flow_out[ni + o] = P.flow_in[ni + o];
-            }
-        }
-        return;
-    }
-    trilateral_block(P.flow_in, P.flow_in + ni, P.flow_med, P.flow_med + ni, P.guide, P.flow_out, P.flow_out + ni,
-                     P.sx_in, P.sy_in, P.tri_s, P.cE, P.cI, P.cS, bx0, by0, smem4);
-}
-
 // Self-test of the bounded barrier: `blocks` blocks wait for `expect` arrivals.
 __global__ void k_barrier_selftest(GridSync* gs, unsigned int expect, unsigned long long limit)
 {
@@ -362,6 +298,7 @@ struct bm_batch {
     std::vector<uint32_t> order;   // internal index -> caller's pair index (ascending working set)
     std::vector<uint32_t> pos;     // caller's pair index -> internal index
     std::vector<size_t> ws;        // working set of each pair (internal order), bytes
+    std::vector<PatternOffsets> pattern_off;  // per pair (internal order), for the per-pair descriptor launches
     int max_fsize = 1, max_tri_s = 0;
     size_t tri_smem = 0;
     int coop_blocks_per_sm = 0, num_sms = 0;
@@ -454,19 +391,23 @@ bm_status enqueue_step(bm_batch* b, const bm_batch_schedule& s)
 bm_status enqueue_wave(bm_batch* b, const bm_batch_schedule& s, int lo, int hi)
 {
     const BatchDev bd = batch_dev(b, lo, hi);
-    const unsigned int t_up = b->pre_up[hi] - b->pre_up[lo], t_in = b->pre_in[hi] - b->pre_in[lo],
-                       t_tri = b->pre_tri[hi] - b->pre_tri[lo];
+    const unsigned int t_up = b->pre_up[hi] - b->pre_up[lo], t_in = b->pre_in[hi] - b->pre_in[lo];
     cudaStream_t st = b->stream;
     const dim3 blk(TX, TY);
     k_b_guide<<<t_in, blk, 0, st>>>(bd);
     BB_CUDA(cudaGetLastError());
+    // descriptors: one launch per pair so each reads its sample offsets from the
+    // parameter space (the single-pair kernel)
     for (int which = 0; which < 2; which++) {
         k_b_upsample<<<t_up, blk, 0, st>>>(bd, which);
         BB_CUDA(cudaGetLastError());
-        BB_NSP(b->nsp, (k_b_features<NSP><<<t_up, blk, 0, st>>>(bd, which)));
-        BB_CUDA(cudaGetLastError());
+        for (int j = lo; j < hi; j++) {
+            const PairDev& d = b->pairs[j];
+            BB_CUDA(features(d.up, d.F[which], d.sx, d.sy, (int)b->N, (int)b->nsp, d.pat, d.rmax, b->pattern_off[j],
+                             which, st));
+        }
     }
-    b->launches += 5;
+    b->launches += 3 + 2 * (hi - lo);
     int cur = 0;
     if (s.persistent) {
         BB_CUDA(cudaMemsetAsync(b->d_sync, 0, sizeof(GridSync), st));
@@ -531,26 +472,25 @@ bm_status enqueue_wave(bm_batch* b, const bm_batch_schedule& s, int lo, int hi)
     }
     k_b_downsample<<<t_in, blk, 0, st>>>(bd, cur);
     BB_CUDA(cudaGetLastError());
-    if (b->filter) {
-        const dim3 g2(t_in, 2);
-#define BB_MED(FSV)                                                        \
-    do {                                                                   \
-        k_b_median<FSV><<<g2, blk, 0, st>>>(bd, 1);                        \
-        k_b_median<FSV><<<g2, blk, 0, st>>>(bd, 0);                        \
-    } while (0)
-        if (b->max_fsize <= 9) BB_MED(9);
-        else if (b->max_fsize <= 13) BB_MED(13);
-        else if (b->max_fsize <= 15) BB_MED(15);
-        else if (b->max_fsize <= 23) BB_MED(23);
-        else if (b->max_fsize <= 31) BB_MED(31);
-        else BB_MED(BM_MAX_MEDIAN);
-#undef BB_MED
-        BB_CUDA(cudaGetLastError());
-        b->launches += 2;
+    b->launches++;
+    // refinement: one launch per pair and stage, each sized to its pair (median
+    // window, trilateral window and shared memory)
+    for (int j = lo; j < hi; j++) {
+        const PairDev& d = b->pairs[j];
+        const bm_params& p = b->prm[b->order[j]];
+        const size_t ni = (size_t)d.sx_in * d.sy_in;
+        if (b->filter) {
+            const int fs = d.fsize == 0 ? 1 : d.fsize;
+            BB_CUDA(median_pass(d.flow_in, d.flow_in + ni, d.tmp, d.tmp + ni, 1, fs, d.sx_in, d.sy_in, st));
+            BB_CUDA(median_pass(d.tmp, d.tmp + ni, d.flow_med, d.flow_med + ni, 0, fs, d.sx_in, d.sy_in, st));
+            BB_CUDA(trilateral(d.flow_in, d.flow_in + ni, d.flow_med, d.flow_med + ni, d.guide, d.flow_out,
+                               d.flow_out + ni, d.sx_in, d.sy_in, d.tri_s, p.sEPE * p.sEPE, p.sI * p.sI,
+                               p.sS * p.sS, st));
+            b->launches += 3;
+        } else {
+            BB_CUDA(cudaMemcpyAsync(d.flow_out, d.flow_in, 2 * ni * sizeof(float), cudaMemcpyDeviceToDevice, st));
+        }
     }
-    k_b_trilateral<<<t_tri, dim3(TX, TRI_TY), b->filter ? b->tri_smem : 0, st>>>(bd, b->filter);
-    BB_CUDA(cudaGetLastError());
-    b->launches += 2;
     return BM_OK;
 }
 
@@ -827,9 +767,7 @@ bm_status bm_batch_create(const bm_params* pairs, uint32_t count, bm_batch** out
         cudaMemsetAsync(b->d_sync, 0, sizeof(GridSync), b->stream) != cudaSuccess ||
         cudaStreamSynchronize(b->stream) != cudaSuccess)
         return fail_clean(bfail(BM_ERR_CUDA, "bm_batch_create: descriptor upload failed"));
-    if (b->tri_smem > 48 * 1024 &&
-        cudaFuncSetAttribute(k_b_trilateral, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->tri_smem) !=
-            cudaSuccess)
+    if (b->filter && ensure_trilateral_smem(b->max_tri_s) != cudaSuccess)
         return fail_clean(bfail(BM_ERR_CUDA, "bm_batch_create: shared-memory opt-in failed"));
     int dev = 0;
     cudaGetDevice(&dev);
@@ -895,6 +833,8 @@ bm_status bm_batch_set_pattern(bm_batch* b, uint32_t pair, const float* h_patter
     const uint32_t j = b->pos[pair];
     PairDev& d = b->pairs[j];
     d.rmax = rmax;
+    if (b->pattern_off.size() != b->count) b->pattern_off.resize(b->count);
+    std::memcpy(b->pattern_off[j].off, off.data(), sizeof(b->pattern_off[j].off));
     BB_CUDA(cudaMemcpyAsync((void*)d.pat, pat.data(), b->N * sizeof(int4), cudaMemcpyHostToDevice, b->stream));
     BB_CUDA(cudaMemcpyAsync((void*)d.off, off.data(), off.size() * sizeof(int2), cudaMemcpyHostToDevice, b->stream));
     if (b->d_pairs)

@@ -76,6 +76,7 @@ cudaError_t flow_to_planes(const uint32_t* flow, float* U, float* V, size_t n, c
 cudaError_t median_pass(const float* inU, const float* inV, float* outU, float* outV,
                         int dir, int fsize, int sx, int sy, cudaStream_t st);
 
+cudaError_t ensure_trilateral_smem(int s);
 cudaError_t trilateral(const float* U, const float* V, const float* Um, const float* Vm,
                        const float* I, float* Uo, float* Vo, int sx, int sy, int s,
                        float sigmaEPE2, float sigmaI2, float sigmaS2, cudaStream_t st);

@@ -384,6 +384,22 @@ cudaError_t median_pass(const float* inU, const float* inV, float* outU, float* 
     return cudaGetLastError();
 }
 
+// The trilateral kernel's dynamic shared-memory opt-in, raised only when a larger
+// window than any before needs it (so launches after the first of a size make no
+// attribute call and can be captured in a graph).
+cudaError_t ensure_trilateral_smem(int s)
+{
+    static int granted[64] = {0};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const int need = (int)tri_smem_bytes(s);
+    if (dev >= 0 && dev < 64 && need <= granted[dev]) return cudaSuccess;
+    e = cudaFuncSetAttribute(k_trilateral_x2, cudaFuncAttributeMaxDynamicSharedMemorySize, need);
+    if (e == cudaSuccess && dev >= 0 && dev < 64) granted[dev] = need;
+    return e;
+}
+
 cudaError_t trilateral(const float* U, const float* V, const float* Um, const float* Vm,
                        const float* I, float* Uo, float* Vo, int sx, int sy, int s,
                        float sigmaEPE2, float sigmaI2, float sigmaS2, cudaStream_t st)
@@ -392,7 +408,7 @@ cudaError_t trilateral(const float* U, const float* V, const float* Um, const fl
     const float cE = tc.cE, cI = tc.cI, cS = tc.cS;
     const size_t smem = tri_smem_bytes(s);
     if (smem <= 220 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(k_trilateral_x2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e = ensure_trilateral_smem(s);
         if (e != cudaSuccess) return e;
         dim3 g((sx + TX - 1) / TX, (sy + TRI_BY - 1) / TRI_BY);
         k_trilateral_x2<<<g, dim3(TX, TRI_TY), smem, st>>>(U, V, Um, Vm, I, Uo, Vo, sx, sy, s, cE, cI, cS);
