@@ -388,8 +388,70 @@ bm_status enqueue_step(bm_batch* b, const bm_batch_schedule& s)
     return BM_OK;
 }
 
+// One pair through the single-pair kernels (parameters in the launch, as a plain
+// context runs it), into the batch's buffers.
+bm_status enqueue_pair(bm_batch* b, const bm_batch_schedule& s, int j)
+{
+    const PairDev& d = b->pairs[j];
+    cudaStream_t st = b->stream;
+    const size_t ni = (size_t)d.sx_in * d.sy_in;
+    const bool resample = d.sx != d.sx_in || d.sy != d.sy_in;
+    BB_CUDA(u8_to_f32(d.frame[0], d.guide, ni, st));
+    int rev = 0;
+    for (int which = 0; which < 2; which++) {
+        const float* up = d.up;
+        if (resample) {
+            BB_CUDA(upsample_u8(d.frame[which], d.up, d.sx_in, d.sy_in, d.sx, d.sy, d.lx, d.ix, d.ly, d.iy, st));
+        } else {
+            BB_CUDA(u8_to_f32(d.frame[which], d.up, ni, st));
+        }
+        BB_CUDA(features(up, d.F[which], d.sx, d.sy, (int)b->N, (int)b->nsp, d.pat, d.rmax, b->pattern_off[j], rev, st));
+        rev ^= s.snake ? 1 : 0;
+    }
+    int cur = 0;
+    BB_CUDA(initialize(d.F[0], d.F[1], d.flow[cur], d.flow[cur ^ 1], d.cost, d.sx, d.sy, (int)b->nsp, 1, rev, st));
+    rev ^= s.snake ? 1 : 0;
+    cur ^= 1;
+    int pd = -1;
+    int levels = 0;
+    for (int q = (int)b->jfMax; q > 0; q /= 2) levels++;
+    for (uint32_t it = 0; it < b->iterations; it++) {
+        int lvl = 0;
+        for (int q = (int)b->jfMax; q > 0; q /= 2, lvl++) {
+            RsArgs rs;
+            rs.enabled = lvl == levels - 1;
+            rs.mode = b->rng;
+            rs.seed = b->seed;
+            rs.call = it;
+            rs.dist = d.dist;
+            BB_CUDA(jump_level(d.F[0], d.F[1], d.flow[cur], d.flow[cur ^ 1], d.cost, d.sx, d.sy, (int)b->nsp, q, pd,
+                               b->doubleProp, rs, rev, st));
+            rev ^= s.snake ? 1 : 0;
+            cur ^= 1;
+        }
+        pd = -pd;
+    }
+    if (resample) {
+        BB_CUDA(downsample(d.flow[cur], d.flow_in, d.flow_in + ni, d.sx, d.sy, d.sx_in, d.sy_in, d.taps, d.P, d.mx,
+                           d.my, d.nnx, d.nny, st));
+    } else {
+        BB_CUDA(flow_to_planes(d.flow[cur], d.flow_in, d.flow_in + ni, ni, st));
+    }
+    b->launches += 6 + (uint64_t)b->iterations * levels;
+    return BM_OK;
+}
+
+bm_status enqueue_refine(bm_batch* b, int lo, int hi);
+
 bm_status enqueue_wave(bm_batch* b, const bm_batch_schedule& s, int lo, int hi)
 {
+    if (s.per_pair) {
+        for (int j = lo; j < hi; j++) {
+            bm_status st = enqueue_pair(b, s, j);
+            if (st != BM_OK) return st;
+        }
+        return enqueue_refine(b, lo, hi);
+    }
     const BatchDev bd = batch_dev(b, lo, hi);
     const unsigned int t_up = b->pre_up[hi] - b->pre_up[lo], t_in = b->pre_in[hi] - b->pre_in[lo];
     cudaStream_t st = b->stream;
@@ -473,8 +535,14 @@ bm_status enqueue_wave(bm_batch* b, const bm_batch_schedule& s, int lo, int hi)
     k_b_downsample<<<t_in, blk, 0, st>>>(bd, cur);
     BB_CUDA(cudaGetLastError());
     b->launches++;
-    // refinement: one launch per pair and stage, each sized to its pair (median
-    // window, trilateral window and shared memory)
+    return enqueue_refine(b, lo, hi);
+}
+
+// Refinement: one launch per pair and stage, each sized to its pair (median window,
+// trilateral window and shared memory).
+bm_status enqueue_refine(bm_batch* b, int lo, int hi)
+{
+    cudaStream_t st = b->stream;
     for (int j = lo; j < hi; j++) {
         const PairDev& d = b->pairs[j];
         const bm_params& p = b->prm[b->order[j]];
@@ -587,6 +655,7 @@ bm_status bm_batch_create(const bm_params* pairs, uint32_t count, bm_batch** out
     b->sched.use_graph = 1;
     b->sched.spin_limit = 1ull << 24;
     b->sched.wave_bytes = 0;
+    b->sched.per_pair = 0;
     {
         std::vector<size_t> ws_api(count);
         for (uint32_t i = 0; i < count; i++) {
@@ -954,6 +1023,7 @@ bm_status bm_batch_autotune(bm_batch* b, const char* cache_path, int reps, char*
             ok &= grab("snake", v) && ((s.snake = (uint32_t)v), true);
             ok &= grab("use_graph", v) && ((s.use_graph = (uint32_t)v), true);
             ok &= grab("wave_bytes", v) && ((s.wave_bytes = v), true);
+            ok &= grab("per_pair", v) && ((s.per_pair = (uint32_t)v), true);
             if (ok) {
                 bm_batch_set_schedule(b, &s);
                 if (report) std::snprintf(report, report_len, "cached: %s", hit.c_str());
@@ -963,10 +1033,20 @@ bm_status bm_batch_autotune(bm_batch* b, const char* cache_path, int reps, char*
     }
     std::vector<bm_batch_schedule> cands;
     const uint64_t MB = 1ull << 20;
+    {
+        bm_batch_schedule s = b->sched;
+        s.per_pair = 1;
+        s.persistent = 0;
+        s.snake = 1;
+        s.use_graph = 1;
+        s.wave_bytes = 0;
+        cands.push_back(s);
+    }
     const uint64_t waves[4] = {0ull, 64 * MB, 96 * MB, 160 * MB};
     for (uint64_t wave : waves) {
         for (uint32_t persistent = 0; persistent <= 1; persistent++) {
             bm_batch_schedule s = b->sched;
+            s.per_pair = 0;
             s.persistent = persistent;
             s.blocks_per_sm = (uint32_t)b->coop_blocks_per_sm;
             s.snake = 1;
@@ -987,7 +1067,8 @@ bm_status bm_batch_autotune(bm_batch* b, const char* cache_path, int reps, char*
         bm_status st = bm_batch_run(b);
         if (st == BM_OK) st = bm_batch_synchronize(b);
         if (st != BM_OK) {
-            rep << "{persistent=" << s.persistent << ",wave=" << (s.wave_bytes >> 20) << "MB: failed} ";
+            rep << "{per_pair=" << s.per_pair << ",persistent=" << s.persistent << ",wave=" << (s.wave_bytes >> 20)
+                << "MB: failed} ";
             continue;
         }
         cudaEventRecord(e0, b->stream);
@@ -997,7 +1078,7 @@ bm_status bm_batch_autotune(bm_batch* b, const char* cache_path, int reps, char*
         float ms = 0;
         cudaEventElapsedTime(&ms, e0, e1);
         ms /= reps;
-        rep << "{persistent=" << s.persistent << ",wave=" << (s.wave_bytes >> 20) << "MB: "
+        rep << "{per_pair=" << s.per_pair << ",persistent=" << s.persistent << ",wave=" << (s.wave_bytes >> 20) << "MB: "
             << (st == BM_OK ? std::to_string(ms) : std::string("failed")) << " ms} ";
         if (st == BM_OK && ms < best_ms) {
             best_ms = ms;
@@ -1011,11 +1092,12 @@ bm_status bm_batch_autotune(bm_batch* b, const char* cache_path, int reps, char*
         std::ofstream out(cache_path, std::ios::app);
         out << "{\"key\": \"" << key << "\", \"persistent\": " << best.persistent << ", \"blocks_per_sm\": "
             << best.blocks_per_sm << ", \"snake\": " << best.snake << ", \"use_graph\": " << best.use_graph
-            << ", \"wave_bytes\": " << best.wave_bytes << ", \"ms\": " << best_ms << "}\n";
+            << ", \"wave_bytes\": " << best.wave_bytes << ", \"per_pair\": " << best.per_pair << ", \"ms\": "
+            << best_ms << "}\n";
     }
     if (report)
-        std::snprintf(report, report_len, "%s-> persistent=%u wave=%lluMB", rep.str().c_str(), best.persistent,
-                      (unsigned long long)(best.wave_bytes >> 20));
+        std::snprintf(report, report_len, "%s-> per_pair=%u persistent=%u wave=%lluMB", rep.str().c_str(),
+                      best.per_pair, best.persistent, (unsigned long long)(best.wave_bytes >> 20));
     return BM_OK;
 }
 

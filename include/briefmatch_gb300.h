@@ -213,6 +213,9 @@ typedef struct bm_batch_schedule {
     uint64_t spin_limit;     /* polls before a grid barrier gives up (BM_ERR_TIMEOUT) */
     uint64_t wave_bytes;     /* run pairs in waves whose working sets sum to at most this
                                 (smallest pairs first, so a wave stays L2-resident); 0 = one wave */
+    uint32_t per_pair;       /* every stage as a launch per pair (the single-pair kernels,
+                                parameters in the launch) instead of union-of-tiles launches */
+    uint32_t reserved;
 } bm_batch_schedule;
 
 bm_status bm_batch_create(const bm_params* pairs, uint32_t count, bm_batch** out);

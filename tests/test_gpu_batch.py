@@ -43,6 +43,8 @@ def _single(params, frames):
     dict(persistent=1, snake=0, use_graph=1),
     dict(persistent=0, snake=1, use_graph=1, wave_bytes=1),          # one pair per wave
     dict(persistent=1, snake=1, use_graph=1, wave_bytes=3 << 20),    # small waves
+    dict(per_pair=1, persistent=0, snake=1, use_graph=1),
+    dict(per_pair=1, persistent=0, snake=0, use_graph=0),
 ])
 def test_batch_equals_single_pairs(sched):
     params, frames = _batch_inputs()
@@ -81,13 +83,13 @@ def test_autotune_and_cache(tmp_path):
     rep = b.autotune(cache, reps=2)
     assert "persistent=" in rep
     line = json.loads(open(cache).read().strip().splitlines()[-1])
-    assert {"key", "persistent", "blocks_per_sm", "snake", "use_graph", "ms"} <= set(line)
+    assert {"key", "persistent", "blocks_per_sm", "snake", "use_graph", "wave_bytes", "per_pair", "ms"} <= set(line)
     chosen = b.schedule()
     b.close()
     b2 = bm.Batch(params)
     rep2 = b2.autotune(cache)
     assert rep2.startswith("cached")
-    assert b2.schedule()["persistent"] == chosen["persistent"]
+    assert all(b2.schedule()[k] == chosen[k] for k in ("persistent", "per_pair", "wave_bytes", "snake"))
     b2.load_frames(b2.pack_frames(frames))
     b2.run()
     b2.synchronize()
