@@ -1,0 +1,640 @@
+// bm_net.cu -- the learned flow proposal: a 6-layer 3x3 convolutional network at
+// quarter resolution that predicts an initial flow and a confidence for PatchMatch.
+//
+//   layer 0: 2 -> 32 channels, ReLU       (input: the two frames, quarter resolution)
+//   layers 1-4: 32 -> 32 channels, ReLU
+//   layer 5: 32 -> 3 channels, linear     (u/4, v/4 in quarter-resolution pixels, confidence logit)
+//
+// Weights and activations are BF16, accumulation FP32, on the tensor cores through
+// mma.sync m16n8k16 implicit-GEMM kernels: forward, backward-data (the forward kernel
+// on the output gradient with flipped, transposed weights) and backward-weights
+// (pixels as the reduction dimension).  Activations are NHWC with the channel count
+// padded to a multiple of 16 (32-byte rows).  Training keeps FP32 master weights and
+// Adam moments; every step repacks the BF16 copies the kernels read.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include <cuda_bf16.h>
+
+#include "bm_internal.h"
+
+namespace {
+
+constexpr int NL = 6;                              // layers
+constexpr int CIN_R[NL] = {2, 32, 32, 32, 32, 32};  // real input channels
+constexpr int COUT_R[NL] = {32, 32, 32, 32, 32, 3};
+constexpr int CIN_P[NL] = {16, 32, 32, 32, 32, 32};  // padded (multiple of 16)
+constexpr int COUT_P[NL] = {32, 32, 32, 32, 32, 8};  // padded (multiple of 8)
+
+constexpr int BW = 16, BH = 8;  // output tile per block: 8 rows x 16 columns, 4 warps
+constexpr int HW = BW + 2, HH = BH + 2;
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1)
+{
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
+{
+    __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<uint32_t*>(&v);
+}
+
+enum Epi { EPI_RELU_BF16 = 0, EPI_LINEAR_F32 = 1, EPI_MASK_BF16 = 2 };
+
+// Y[p, co] = sum_{tap, ci} X[p + tap - 1, ci] * W[tap][co][ci]  (+ bias, ReLU) -- or,
+// for the backward-data pass, the same product followed by the ReLU mask of `act`.
+// X: [B][h][w][CINP] bf16; W: [9][COUTP][CINP] bf16; out per EPI.
+template <int CINP, int COUTP, int EPI>
+__global__ void __launch_bounds__(128) k_conv(const __nv_bfloat16* __restrict__ X, const __nv_bfloat16* __restrict__ W,
+                                              const float* __restrict__ bias, const __nv_bfloat16* __restrict__ act,
+                                              void* __restrict__ out, int h, int w, int cout_real, int out_stride)
+{
+    constexpr int SP = CINP + 8;  // smem pixel stride (bf16): conflict-free fragment loads
+    constexpr int NT = COUTP / 8;
+    __shared__ __align__(16) __nv_bfloat16 s_in[HH * HW * SP];
+    __shared__ __align__(16) __nv_bfloat16 s_w[9 * COUTP * SP];
+    const int tid = threadIdx.x;
+    const int x0 = blockIdx.x * BW, y0 = blockIdx.y * BH, b = blockIdx.z;
+    const __nv_bfloat16* Xb = X + (size_t)b * h * w * CINP;
+    // stage the input tile with a one-pixel zero halo, 16 bytes at a time
+    constexpr int VPP = CINP / 8;  // 16-byte vectors per pixel
+    for (int k = tid; k < HH * HW * VPP; k += 128) {
+        const int pix = k / VPP, v = k - pix * VPP;
+        const int hy = pix / HW, hx = pix - hy * HW;
+        const int gy = y0 + hy - 1, gx = x0 + hx - 1;
+        uint4 val = make_uint4(0, 0, 0, 0);
+        if (gy >= 0 && gy < h && gx >= 0 && gx < w)
+            val = *reinterpret_cast<const uint4*>(Xb + ((size_t)gy * w + gx) * CINP + v * 8);
+        *reinterpret_cast<uint4*>(s_in + pix * SP + v * 8) = val;
+    }
+    for (int k = tid; k < 9 * COUTP * VPP; k += 128) {
+        const int row = k / VPP, v = k - row * VPP;
+        *reinterpret_cast<uint4*>(s_w + row * SP + v * 8) = *reinterpret_cast<const uint4*>(W + (size_t)row * CINP + v * 8);
+    }
+    __syncthreads();
+
+    const int warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
+    const uint32_t* si = reinterpret_cast<const uint32_t*>(s_in);
+    const uint32_t* sw = reinterpret_cast<const uint32_t*>(s_w);
+    float acc[2][NT][4];
+#pragma unroll
+    for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+        for (int nt = 0; nt < NT; nt++)
+#pragma unroll
+            for (int q = 0; q < 4; q++) acc[mt][nt][q] = 0.0f;
+
+#pragma unroll
+    for (int tap = 0; tap < 9; tap++) {
+        const int dy = tap / 3, dx = tap - dy * 3;
+#pragma unroll
+        for (int kc = 0; kc < CINP / 16; kc++) {
+            uint32_t bf[NT][2];
+#pragma unroll
+            for (int nt = 0; nt < NT; nt++) {
+                const int base = ((tap * COUTP + nt * 8 + g) * SP + kc * 16 + 2 * t) >> 1;
+                bf[nt][0] = sw[base];
+                bf[nt][1] = sw[base + 4];
+            }
+#pragma unroll
+            for (int mt = 0; mt < 2; mt++) {
+                const int r = warp * 2 + mt;  // output row within the tile
+                const int p0 = ((r + dy) * HW + g + dx) * SP + kc * 16 + 2 * t;
+                const int p8 = ((r + dy) * HW + g + 8 + dx) * SP + kc * 16 + 2 * t;
+                uint32_t a[4];
+                a[0] = si[p0 >> 1];
+                a[1] = si[p8 >> 1];
+                a[2] = si[(p0 >> 1) + 4];
+                a[3] = si[(p8 >> 1) + 4];
+#pragma unroll
+                for (int nt = 0; nt < NT; nt++) mma_bf16(acc[mt][nt], a, bf[nt][0], bf[nt][1]);
+            }
+        }
+    }
+    // epilogue: C fragment (row g / g+8 = pixel column, cols 2t, 2t+1 = channels)
+#pragma unroll
+    for (int mt = 0; mt < 2; mt++) {
+        const int y = y0 + warp * 2 + mt;
+        if (y >= h) continue;
+#pragma unroll
+        for (int half = 0; half < 2; half++) {
+            const int x = x0 + g + half * 8;
+            if (x >= w) continue;
+            const size_t pix = ((size_t)b * h + y) * w + x;
+#pragma unroll
+            for (int nt = 0; nt < NT; nt++) {
+                const int co = nt * 8 + 2 * t;
+                float v0 = acc[mt][nt][half * 2 + 0], v1 = acc[mt][nt][half * 2 + 1];
+                if constexpr (EPI == EPI_RELU_BF16) {
+                    v0 = fmaxf(v0 + bias[co], 0.0f);
+                    v1 = fmaxf(v1 + bias[co + 1], 0.0f);
+                    reinterpret_cast<uint32_t*>(out)[(pix * out_stride + co) >> 1] = pack_bf16(v0, v1);
+                } else if constexpr (EPI == EPI_MASK_BF16) {
+                    const __nv_bfloat162 m = *reinterpret_cast<const __nv_bfloat162*>(act + pix * out_stride + co);
+                    v0 = __bfloat162float(m.x) > 0.0f ? v0 : 0.0f;
+                    v1 = __bfloat162float(m.y) > 0.0f ? v1 : 0.0f;
+                    reinterpret_cast<uint32_t*>(out)[(pix * out_stride + co) >> 1] = pack_bf16(v0, v1);
+                } else {
+                    float* o = reinterpret_cast<float*>(out) + pix * out_stride;
+                    if (co < cout_real) o[co] = v0 + bias[co];
+                    if (co + 1 < cout_real) o[co + 1] = v1 + bias[co + 1];
+                }
+            }
+        }
+    }
+}
+
+// dW[co][tap][ci] += sum_p dY[p, co] * X[p + tap - 1, ci] and db[co] += sum_p dY[p, co]
+// over one 8x16 tile: A = dY^T (16 output channels x 16 pixels of one tile row),
+// B = the shifted input (16 pixels x 8 input channels).  Each warp owns taps
+// w, w+4, w+8.  Partial sums of the tile are added to the FP32 gradients atomically.
+template <int CINP, int COUTD>
+__global__ void __launch_bounds__(128) k_conv_wgrad(const __nv_bfloat16* __restrict__ X,
+                                                    const __nv_bfloat16* __restrict__ dY, int dy_stride, int h, int w,
+                                                    float* __restrict__ dW, float* __restrict__ db, int cin_real,
+                                                    int cout_real)
+{
+    constexpr int PX = BW * BH;        // 128 pixels
+    constexpr int SPD = PX + 8;        // dY^T row stride (bf16)
+    constexpr int SPX = HH * HW + 8;   // X^T row stride (bf16)
+    constexpr int MT = COUTD / 16, NT = CINP / 8;
+    __shared__ __align__(16) __nv_bfloat16 s_dy[COUTD * SPD];
+    __shared__ __align__(16) __nv_bfloat16 s_x[CINP * SPX];
+    const int tid = threadIdx.x;
+    const int x0 = blockIdx.x * BW, y0 = blockIdx.y * BH, b = blockIdx.z;
+    for (int k = tid; k < COUTD * PX; k += 128) {
+        const int co = k / PX, p = k - co * PX;
+        const int y = y0 + p / BW, x = x0 + (p % BW);
+        __nv_bfloat16 v = __float2bfloat16(0.0f);
+        if (co < cout_real && y < h && x < w) v = dY[(((size_t)b * h + y) * w + x) * dy_stride + co];
+        s_dy[co * SPD + p] = v;
+    }
+    for (int k = tid; k < CINP * HH * HW; k += 128) {
+        const int ci = k / (HH * HW), p = k - ci * (HH * HW);
+        const int gy = y0 + p / HW - 1, gx = x0 + (p % HW) - 1;
+        __nv_bfloat16 v = __float2bfloat16(0.0f);
+        if (gy >= 0 && gy < h && gx >= 0 && gx < w) v = X[(((size_t)b * h + gy) * w + gx) * CINP + ci];
+        s_x[ci * SPX + p] = v;
+    }
+    __syncthreads();
+    // bias gradient
+    for (int co = tid; co < cout_real; co += 128) {
+        float s = 0.0f;
+        for (int p = 0; p < PX; p++) s += __bfloat162float(s_dy[co * SPD + p]);
+        atomicAdd(db + co, s);
+    }
+    const int warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
+    const unsigned short* sx16 = reinterpret_cast<const unsigned short*>(s_x);
+    const uint32_t* sdy = reinterpret_cast<const uint32_t*>(s_dy);
+    for (int tap = warp; tap < 9; tap += 4) {
+        const int dyy = tap / 3, dxx = tap - dyy * 3;
+        float acc[MT][NT][4];
+#pragma unroll
+        for (int mt = 0; mt < MT; mt++)
+#pragma unroll
+            for (int nt = 0; nt < NT; nt++)
+#pragma unroll
+                for (int q = 0; q < 4; q++) acc[mt][nt][q] = 0.0f;
+#pragma unroll 2
+        for (int ks = 0; ks < BH; ks++) {  // one tile row of 16 pixels per k-step
+            uint32_t a[MT][4];
+#pragma unroll
+            for (int mt = 0; mt < MT; mt++) {
+                const int r0 = (mt * 16 + g) * SPD + ks * 16 + 2 * t;
+                const int r8 = (mt * 16 + g + 8) * SPD + ks * 16 + 2 * t;
+                a[mt][0] = sdy[r0 >> 1];
+                a[mt][1] = sdy[r8 >> 1];
+                a[mt][2] = sdy[(r0 >> 1) + 4];
+                a[mt][3] = sdy[(r8 >> 1) + 4];
+            }
+#pragma unroll
+            for (int nt = 0; nt < NT; nt++) {
+                const int ci = nt * 8 + g;
+                const int row = (ks + dyy) * HW + dxx;  // shifted input row for pixels 0..15
+                const int base = ci * SPX + row + 2 * t;
+                const uint32_t b0 = (uint32_t)sx16[base] | ((uint32_t)sx16[base + 1] << 16);
+                const uint32_t b1 = (uint32_t)sx16[base + 8] | ((uint32_t)sx16[base + 9] << 16);
+#pragma unroll
+                for (int mt = 0; mt < MT; mt++) mma_bf16(acc[mt][nt], a[mt], b0, b1);
+            }
+        }
+        // C fragment: rows g / g+8 = output channel, cols 2t, 2t+1 = input channel
+#pragma unroll
+        for (int mt = 0; mt < MT; mt++)
+#pragma unroll
+            for (int nt = 0; nt < NT; nt++)
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const int co = mt * 16 + g + (q >> 1) * 8;
+                    const int ci = nt * 8 + 2 * t + (q & 1);
+                    if (co < cout_real && ci < cin_real)
+                        atomicAdd(dW + ((size_t)co * 9 + tap) * cin_real + ci, acc[mt][nt][q]);
+                }
+    }
+}
+
+// Two frames -> network input: 4x4 box average of each frame, scaled to [-1, 1],
+// channels 0 and 1 of a 16-channel NHWC bf16 image (the rest zero).
+__global__ void k_net_input(const uint8_t* __restrict__ f0, const uint8_t* __restrict__ f1, int W, int H,
+                            __nv_bfloat16* __restrict__ out, int w4, int h4)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= w4 || y >= h4) return;
+    float s0 = 0, s1 = 0;
+    int n = 0;
+    for (int j = 0; j < 4; j++)
+        for (int i = 0; i < 4; i++) {
+            const int xx = min(W - 1, x * 4 + i), yy = min(H - 1, y * 4 + j);
+            s0 += f0[(size_t)yy * W + xx];
+            s1 += f1[(size_t)yy * W + xx];
+            n++;
+        }
+    uint4* o = reinterpret_cast<uint4*>(out + ((size_t)y * w4 + x) * 16);
+    const float a = s0 / n / 127.5f - 1.0f, c = s1 / n / 127.5f - 1.0f;
+    o[0] = make_uint4(pack_bf16(a, c), 0, 0, 0);
+    o[1] = make_uint4(0, 0, 0, 0);
+}
+
+// Loss of the head against BriefMatch's flow: smooth-L1 on (u, v) in quarter
+// resolution pixels and binary cross-entropy of the confidence against "the
+// predicted vector is within tau of the target", averaged over valid pixels.
+// Writes dY (bf16, 16 channels) and adds the loss terms to loss[0..2].
+__global__ void k_net_loss(const float* __restrict__ pred, const float* __restrict__ target, size_t n,
+                           __nv_bfloat16* __restrict__ dY, float inv_count, float tau, float wconf,
+                           float* __restrict__ loss)
+{
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    float lf = 0, lc = 0, acc = 0;
+    if (i < n) {
+        const float u = pred[i * 3], v = pred[i * 3 + 1], c = pred[i * 3 + 2];
+        const float tu = target[i * 3], tv = target[i * 3 + 1], valid = target[i * 3 + 2];
+        const float du = u - tu, dv = v - tv;
+        auto sl1 = [](float d, float& g) {
+            const float a = fabsf(d);
+            if (a < 1.0f) {
+                g = d;
+                return 0.5f * d * d;
+            }
+            g = d > 0 ? 1.0f : -1.0f;
+            return a - 0.5f;
+        };
+        float gu, gv;
+        lf = (sl1(du, gu) + sl1(dv, gv)) * valid;
+        const float label = (fabsf(du) + fabsf(dv) < tau) ? 1.0f : 0.0f;
+        const float sig = 1.0f / (1.0f + expf(-c));
+        lc = valid * (fmaxf(c, 0.0f) - c * label + log1pf(expf(-fabsf(c))));
+        acc = valid * label;
+        uint4* o = reinterpret_cast<uint4*>(dY + i * 16);
+        o[0] = make_uint4(pack_bf16(gu * valid * inv_count, gv * valid * inv_count),
+                          pack_bf16(wconf * (sig - label) * valid * inv_count, 0.0f), 0, 0);
+        o[1] = make_uint4(0, 0, 0, 0);
+    }
+    // block reduction of the loss terms
+    __shared__ float red[3][256];
+    red[0][threadIdx.x] = lf;
+    red[1][threadIdx.x] = lc;
+    red[2][threadIdx.x] = acc;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if ((int)threadIdx.x < s)
+            for (int k = 0; k < 3; k++) red[k][threadIdx.x] += red[k][threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        atomicAdd(loss + 0, red[0][0] * inv_count);
+        atomicAdd(loss + 1, red[1][0] * inv_count);
+        atomicAdd(loss + 2, red[2][0] * inv_count);
+    }
+}
+
+// Adam on the FP32 master parameters (Kingma & Ba, ICLR 2015).
+__global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m, float* __restrict__ v,
+                       size_t n, float lr, float b1, float b2, float eps, float c1, float c2, float wd)
+{
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float gi = g[i] + wd * p[i];
+    const float mi = b1 * m[i] + (1.0f - b1) * gi;
+    const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    p[i] -= lr * (mi * c1) / (sqrtf(vi * c2) + eps);
+}
+
+// FP32 master parameters of one layer -> the BF16 forward layout W[tap][COUTP][CINP]
+// and the backward-data layout Wb[tap][CINP_as_out][COUTP16_as_in] (taps flipped).
+__global__ void k_pack_layer(const float* __restrict__ master, int cin, int cout, int cinp, int coutp, int coutp16,
+                             __nv_bfloat16* __restrict__ Wf, __nv_bfloat16* __restrict__ Wb)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nf = 9 * coutp * cinp;
+    if (i < nf) {
+        const int tap = i / (coutp * cinp), r = i - tap * coutp * cinp, co = r / cinp, ci = r - co * cinp;
+        const float v = (co < cout && ci < cin) ? master[((size_t)co * 9 + tap) * cin + ci] : 0.0f;
+        Wf[i] = __float2bfloat16(v);
+    }
+    const int nb = 9 * cinp * coutp16;
+    if (Wb && i < nb) {
+        const int tap = i / (cinp * coutp16), r = i - tap * cinp * coutp16, ci = r / coutp16, co = r - ci * coutp16;
+        const int ftap = 8 - tap;
+        const float v = (co < cout && ci < cin) ? master[((size_t)co * 9 + ftap) * cin + ci] : 0.0f;
+        Wb[i] = __float2bfloat16(v);
+    }
+}
+
+template <int CINP, int COUTP, int EPI>
+cudaError_t launch_conv(const __nv_bfloat16* X, const __nv_bfloat16* W, const float* bias, const __nv_bfloat16* act,
+                        void* out, int B, int h, int w, int cout_real, int out_stride, cudaStream_t st)
+{
+    dim3 g((w + BW - 1) / BW, (h + BH - 1) / BH, B);
+    k_conv<CINP, COUTP, EPI><<<g, 128, 0, st>>>(X, W, bias, act, out, h, w, cout_real, out_stride);
+    return cudaGetLastError();
+}
+
+template <int CINP, int COUTD>
+cudaError_t launch_wgrad(const __nv_bfloat16* X, const __nv_bfloat16* dY, int dy_stride, int B, int h, int w,
+                         float* dW, float* db, int cin_real, int cout_real, cudaStream_t st)
+{
+    dim3 g((w + BW - 1) / BW, (h + BH - 1) / BH, B);
+    k_conv_wgrad<CINP, COUTD><<<g, 128, 0, st>>>(X, dY, dy_stride, h, w, dW, db, cin_real, cout_real);
+    return cudaGetLastError();
+}
+
+size_t layer_w_count(int l) { return (size_t)COUT_R[l] * 9 * CIN_R[l]; }
+size_t layer_param_count(int l) { return layer_w_count(l) + COUT_R[l]; }
+
+}  // namespace
+
+struct bm_net {
+    uint32_t maxB = 0, maxh = 0, maxw = 0;
+    size_t nparam = 0;
+    size_t poff[NL] = {};         // offset of layer l's weights in the parameter vector (bias follows)
+    float* d_master = nullptr;    // FP32 parameters
+    float* d_grad = nullptr;
+    float* d_m = nullptr;
+    float* d_v = nullptr;
+    __nv_bfloat16* d_wf[NL] = {};
+    __nv_bfloat16* d_wb[NL] = {};
+    __nv_bfloat16* d_in = nullptr;      // [B][h][w][16]
+    __nv_bfloat16* d_act[NL - 1] = {};  // outputs of layers 0..4, [B][h][w][32]
+    __nv_bfloat16* d_dy[2] = {};        // gradient ping-pong, [B][h][w][32]
+    float* d_out = nullptr;             // [B][h][w][3]
+    float* d_loss = nullptr;            // 3 floats
+    uint64_t step = 0;
+    bool packed = false;
+};
+
+namespace {
+
+bm_status nfail(bm_status st, const char* msg)
+{
+    bmk::set_error_text(msg);
+    return st;
+}
+
+#define BN_CUDA(call)                                                       \
+    do {                                                                    \
+        cudaError_t e_ = (call);                                            \
+        if (e_ != cudaSuccess) {                                            \
+            char b_[256];                                                   \
+            std::snprintf(b_, sizeof(b_), "bm_net: %s (line %d)", cudaGetErrorString(e_), __LINE__); \
+            return nfail(BM_ERR_CUDA, b_);                                  \
+        }                                                                   \
+    } while (0)
+
+bm_status pack_weights(bm_net* n, cudaStream_t st)
+{
+    for (int l = 0; l < NL; l++) {
+        const int coutp16 = COUT_P[l] < 16 ? 16 : COUT_P[l];
+        const int cnt = 9 * CIN_P[l] * coutp16 > 9 * COUT_P[l] * CIN_P[l] ? 9 * CIN_P[l] * coutp16 : 9 * COUT_P[l] * CIN_P[l];
+        k_pack_layer<<<(cnt + 255) / 256, 256, 0, st>>>(n->d_master + n->poff[l], CIN_R[l], COUT_R[l], CIN_P[l], COUT_P[l],
+                                                          coutp16, n->d_wf[l], l > 0 ? n->d_wb[l] : nullptr);
+        BN_CUDA(cudaGetLastError());
+    }
+    n->packed = true;
+    return BM_OK;
+}
+
+bm_status check_dims(bm_net* n, uint32_t B, uint32_t h, uint32_t w)
+{
+    if (B == 0 || h == 0 || w == 0 || B > n->maxB || (size_t)h * w > (size_t)n->maxh * n->maxw)
+        return nfail(BM_ERR_LIMIT, "bm_net: batch or image size beyond the network's buffers");
+    return BM_OK;
+}
+
+bm_status forward(bm_net* n, uint32_t B, uint32_t h, uint32_t w, cudaStream_t st)
+{
+    if (!n->packed) {
+        bm_status s = pack_weights(n, st);
+        if (s != BM_OK) return s;
+    }
+    const int Bi = (int)B, hi = (int)h, wi = (int)w;
+    BN_CUDA((launch_conv<16, 32, EPI_RELU_BF16>(n->d_in, n->d_wf[0], n->d_master + n->poff[0] + layer_w_count(0),
+                                                nullptr, n->d_act[0], Bi, hi, wi, 32, 32, st)));
+    for (int l = 1; l <= 4; l++)
+        BN_CUDA((launch_conv<32, 32, EPI_RELU_BF16>(n->d_act[l - 1], n->d_wf[l],
+                                                    n->d_master + n->poff[l] + layer_w_count(l), nullptr, n->d_act[l],
+                                                    Bi, hi, wi, 32, 32, st)));
+    BN_CUDA((launch_conv<32, 8, EPI_LINEAR_F32>(n->d_act[4], n->d_wf[5], n->d_master + n->poff[5] + layer_w_count(5),
+                                                nullptr, n->d_out, Bi, hi, wi, 3, 3, st)));
+    return BM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t bm_net_param_count(void)
+{
+    size_t s = 0;
+    for (int l = 0; l < NL; l++) s += layer_param_count(l);
+    return s;
+}
+
+bm_status bm_net_create(uint32_t max_batch, uint32_t max_h4, uint32_t max_w4, bm_net** out)
+{
+    if (!out || max_batch == 0 || max_h4 == 0 || max_w4 == 0) return nfail(BM_ERR_INVALID, "bm_net_create: bad size");
+    bm_net* n = new bm_net();
+    n->maxB = max_batch;
+    n->maxh = max_h4;
+    n->maxw = max_w4;
+    size_t off = 0;
+    for (int l = 0; l < NL; l++) {
+        n->poff[l] = off;
+        off += layer_param_count(l);
+    }
+    n->nparam = off;
+    const size_t px = (size_t)max_batch * max_h4 * max_w4;
+    bool ok = cudaMalloc((void**)&n->d_master, off * 4) == cudaSuccess &&
+              cudaMalloc((void**)&n->d_grad, off * 4) == cudaSuccess &&
+              cudaMalloc((void**)&n->d_m, off * 4) == cudaSuccess && cudaMalloc((void**)&n->d_v, off * 4) == cudaSuccess &&
+              cudaMalloc((void**)&n->d_in, px * 16 * 2) == cudaSuccess &&
+              cudaMalloc((void**)&n->d_out, px * 3 * 4) == cudaSuccess &&
+              cudaMalloc((void**)&n->d_loss, 4 * 4) == cudaSuccess &&
+              cudaMalloc((void**)&n->d_dy[0], px * 32 * 2) == cudaSuccess &&
+              cudaMalloc((void**)&n->d_dy[1], px * 32 * 2) == cudaSuccess;
+    for (int l = 0; ok && l < NL - 1; l++) ok = cudaMalloc((void**)&n->d_act[l], px * 32 * 2) == cudaSuccess;
+    for (int l = 0; ok && l < NL; l++) {
+        const int coutp16 = COUT_P[l] < 16 ? 16 : COUT_P[l];
+        ok = cudaMalloc((void**)&n->d_wf[l], (size_t)9 * COUT_P[l] * CIN_P[l] * 2) == cudaSuccess &&
+             cudaMalloc((void**)&n->d_wb[l], (size_t)9 * CIN_P[l] * coutp16 * 2) == cudaSuccess;
+    }
+    if (!ok) {
+        bm_net_destroy(n);
+        return nfail(BM_ERR_NOMEM, "bm_net_create: device allocation failed");
+    }
+    cudaMemset(n->d_m, 0, off * 4);
+    cudaMemset(n->d_v, 0, off * 4);
+    cudaMemset(n->d_dy[0], 0, px * 32 * 2);
+    cudaMemset(n->d_dy[1], 0, px * 32 * 2);
+    // He initialisation from a fixed-seed LCG (deterministic across machines)
+    std::vector<float> p(off, 0.0f);
+    uint64_t s = 0x9E3779B97F4A7C15ull;
+    auto uni = [&]() {
+        s = s * 6364136223846793005ull + 1442695040888963407ull;
+        return ((s >> 40) + 0.5) / 16777216.0;
+    };
+    for (int l = 0; l < NL; l++) {
+        const double bound = std::sqrt(6.0 / (9.0 * CIN_R[l])) * (l == NL - 1 ? 0.1 : 1.0);
+        for (size_t k = 0; k < layer_w_count(l); k++) p[n->poff[l] + k] = (float)((2 * uni() - 1) * bound);
+    }
+    if (cudaMemcpy(n->d_master, p.data(), off * 4, cudaMemcpyHostToDevice) != cudaSuccess) {
+        bm_net_destroy(n);
+        return nfail(BM_ERR_CUDA, "bm_net_create: parameter upload failed");
+    }
+    *out = n;
+    return BM_OK;
+}
+
+bm_status bm_net_destroy(bm_net* n)
+{
+    if (!n) return BM_OK;
+    void* ptrs[] = {n->d_master, n->d_grad, n->d_m, n->d_v, n->d_in, n->d_out, n->d_loss, n->d_dy[0], n->d_dy[1]};
+    for (void* q : ptrs)
+        if (q) cudaFree(q);
+    for (int l = 0; l < NL; l++) {
+        if (n->d_wf[l]) cudaFree(n->d_wf[l]);
+        if (n->d_wb[l]) cudaFree(n->d_wb[l]);
+        if (l < NL - 1 && n->d_act[l]) cudaFree(n->d_act[l]);
+    }
+    delete n;
+    return BM_OK;
+}
+
+bm_status bm_net_set_params(bm_net* n, const float* h_params, size_t count)
+{
+    if (!n || !h_params || count != n->nparam) return nfail(BM_ERR_INVALID, "bm_net_set_params: wrong parameter count");
+    BN_CUDA(cudaMemcpy(n->d_master, h_params, count * 4, cudaMemcpyHostToDevice));
+    BN_CUDA(cudaMemset(n->d_m, 0, count * 4));
+    BN_CUDA(cudaMemset(n->d_v, 0, count * 4));
+    n->step = 0;
+    n->packed = false;
+    return BM_OK;
+}
+
+bm_status bm_net_get_params(bm_net* n, float* h_params, size_t count)
+{
+    if (!n || !h_params || count != n->nparam) return nfail(BM_ERR_INVALID, "bm_net_get_params: wrong parameter count");
+    BN_CUDA(cudaMemcpy(h_params, n->d_master, count * 4, cudaMemcpyDeviceToHost));
+    return BM_OK;
+}
+
+// Network input of image b from two 8-bit frames W x H (device).
+bm_status bm_net_prepare(bm_net* n, uint32_t b, const uint8_t* d_f0, const uint8_t* d_f1, uint32_t W, uint32_t H,
+                         void* stream)
+{
+    if (!n || !d_f0 || !d_f1) return nfail(BM_ERR_INVALID, "bm_net_prepare: null argument");
+    const uint32_t w4 = W / 4, h4 = H / 4;
+    if (b >= n->maxB || (size_t)w4 * h4 > (size_t)n->maxh * n->maxw || w4 == 0 || h4 == 0)
+        return nfail(BM_ERR_LIMIT, "bm_net_prepare: beyond the network's buffers");
+    dim3 blk(32, 8), g((w4 + 31) / 32, (h4 + 7) / 8);
+    k_net_input<<<g, blk, 0, (cudaStream_t)stream>>>(d_f0, d_f1, (int)W, (int)H, n->d_in + (size_t)b * h4 * w4 * 16,
+                                                     (int)w4, (int)h4);
+    BN_CUDA(cudaGetLastError());
+    return BM_OK;
+}
+
+// Raw network input (bf16 NHWC, 16 channels) for tests.
+bm_status bm_net_set_input(bm_net* n, const uint16_t* d_in, uint32_t B, uint32_t h, uint32_t w, void* stream)
+{
+    if (!n || !d_in) return nfail(BM_ERR_INVALID, "bm_net_set_input: null");
+    bm_status s = check_dims(n, B, h, w);
+    if (s != BM_OK) return s;
+    BN_CUDA(cudaMemcpyAsync(n->d_in, d_in, (size_t)B * h * w * 16 * 2, cudaMemcpyDeviceToDevice, (cudaStream_t)stream));
+    return BM_OK;
+}
+
+bm_status bm_net_forward(bm_net* n, uint32_t B, uint32_t h, uint32_t w, float* d_out, void* stream)
+{
+    if (!n) return nfail(BM_ERR_INVALID, "bm_net_forward: null");
+    bm_status s = check_dims(n, B, h, w);
+    if (s != BM_OK) return s;
+    cudaStream_t st = (cudaStream_t)stream;
+    s = forward(n, B, h, w, st);
+    if (s != BM_OK) return s;
+    if (d_out) BN_CUDA(cudaMemcpyAsync(d_out, n->d_out, (size_t)B * h * w * 3 * 4, cudaMemcpyDeviceToDevice, st));
+    return BM_OK;
+}
+
+// Forward, loss against d_target ([B][h][w][3]: u, v in quarter-resolution pixels and
+// a validity weight), backward into the FP32 gradient (d_grad_out, optional copy),
+// and -- when lr > 0 -- one Adam step.  h_loss receives (flow loss, confidence loss,
+// fraction of confident labels).
+bm_status bm_net_train_step(bm_net* n, uint32_t B, uint32_t h, uint32_t w, const float* d_target, float lr,
+                            float* d_grad_out, float* h_loss, void* stream)
+{
+    if (!n || !d_target) return nfail(BM_ERR_INVALID, "bm_net_train_step: null");
+    bm_status s = check_dims(n, B, h, w);
+    if (s != BM_OK) return s;
+    cudaStream_t st = (cudaStream_t)stream;
+    s = forward(n, B, h, w, st);
+    if (s != BM_OK) return s;
+    const size_t px = (size_t)B * h * w;
+    const int Bi = (int)B, hi = (int)h, wi = (int)w;
+    BN_CUDA(cudaMemsetAsync(n->d_grad, 0, n->nparam * 4, st));
+    BN_CUDA(cudaMemsetAsync(n->d_loss, 0, 4 * 4, st));
+    k_net_loss<<<(unsigned)((px + 255) / 256), 256, 0, st>>>(n->d_out, d_target, px, n->d_dy[0], 1.0f / (float)px, 1.0f,
+                                                             0.25f, n->d_loss);
+    BN_CUDA(cudaGetLastError());
+    // layer 5: dY (16 padded channels, 3 real) -> dW5, and dX into the ReLU mask of act[4]
+    float* g = n->d_grad;
+    BN_CUDA((launch_wgrad<32, 16>(n->d_act[4], n->d_dy[0], 16, Bi, hi, wi, g + n->poff[5], g + n->poff[5] + layer_w_count(5),
+                                  32, 3, st)));
+    BN_CUDA((launch_conv<16, 32, EPI_MASK_BF16>(n->d_dy[0], n->d_wb[5], nullptr, n->d_act[4], n->d_dy[1], Bi, hi, wi, 32,
+                                                32, st)));
+    int cur = 1;
+    for (int l = 4; l >= 1; l--) {
+        BN_CUDA((launch_wgrad<32, 32>(n->d_act[l - 1], n->d_dy[cur], 32, Bi, hi, wi, g + n->poff[l],
+                                      g + n->poff[l] + layer_w_count(l), 32, 32, st)));
+        BN_CUDA((launch_conv<32, 32, EPI_MASK_BF16>(n->d_dy[cur], n->d_wb[l], nullptr, n->d_act[l - 1], n->d_dy[cur ^ 1],
+                                                    Bi, hi, wi, 32, 32, st)));
+        cur ^= 1;
+    }
+    BN_CUDA((launch_wgrad<16, 32>(n->d_in, n->d_dy[cur], 32, Bi, hi, wi, g + n->poff[0], g + n->poff[0] + layer_w_count(0),
+                                  2, 32, st)));
+    if (d_grad_out) BN_CUDA(cudaMemcpyAsync(d_grad_out, g, n->nparam * 4, cudaMemcpyDeviceToDevice, st));
+    if (lr > 0) {
+        n->step++;
+        const float b1 = 0.9f, b2 = 0.999f;
+        const float c1 = 1.0f / (1.0f - std::pow(b1, (float)n->step)), c2 = 1.0f / (1.0f - std::pow(b2, (float)n->step));
+        k_adam<<<(unsigned)((n->nparam + 255) / 256), 256, 0, st>>>(n->d_master, g, n->d_m, n->d_v, n->nparam, lr, b1, b2,
+                                                                    1e-8f, c1, c2, 0.0f);
+        BN_CUDA(cudaGetLastError());
+        s = pack_weights(n, st);
+        if (s != BM_OK) return s;
+    }
+    if (h_loss) {
+        BN_CUDA(cudaMemcpyAsync(h_loss, n->d_loss, 3 * 4, cudaMemcpyDeviceToHost, st));
+        BN_CUDA(cudaStreamSynchronize(st));
+    }
+    return BM_OK;
+}
+
+}  // extern "C"

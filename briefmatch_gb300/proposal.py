@@ -1,0 +1,99 @@
+"""The learned flow proposal over the engine's C ABI (bm_net_*).
+
+ProposalNet wraps the 6-layer BF16 convolutional network: preparing inputs from
+8-bit frames, the forward pass and a training step (forward, loss, backward and Adam
+on the tensor-core kernels).  Parameters save and load as a flat float32 file.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import check, lib
+
+_declared = False
+
+
+def _declare():
+    global _declared
+    if _declared:
+        return
+    L = lib()
+    c = ctypes
+    sig = {
+        "bm_net_param_count": (c.c_size_t, []),
+        "bm_net_create": (c.c_int, [c.c_uint32, c.c_uint32, c.c_uint32, c.POINTER(c.c_void_p)]),
+        "bm_net_destroy": (c.c_int, [c.c_void_p]),
+        "bm_net_set_params": (c.c_int, [c.c_void_p, c.c_void_p, c.c_size_t]),
+        "bm_net_get_params": (c.c_int, [c.c_void_p, c.c_void_p, c.c_size_t]),
+        "bm_net_prepare": (c.c_int, [c.c_void_p, c.c_uint32, c.c_void_p, c.c_void_p, c.c_uint32, c.c_uint32, c.c_void_p]),
+        "bm_net_set_input": (c.c_int, [c.c_void_p, c.c_void_p, c.c_uint32, c.c_uint32, c.c_uint32, c.c_void_p]),
+        "bm_net_forward": (c.c_int, [c.c_void_p, c.c_uint32, c.c_uint32, c.c_uint32, c.c_void_p, c.c_void_p]),
+        "bm_net_train_step": (c.c_int, [c.c_void_p, c.c_uint32, c.c_uint32, c.c_uint32, c.c_void_p, c.c_float,
+                                        c.c_void_p, c.c_void_p, c.c_void_p]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _declared = True
+
+
+def param_count():
+    _declare()
+    return int(lib().bm_net_param_count())
+
+
+class ProposalNet:
+    def __init__(self, max_batch, max_h4, max_w4):
+        _declare()
+        self._n = ctypes.c_void_p(None)
+        check(lib().bm_net_create(max_batch, max_h4, max_w4, ctypes.byref(self._n)))
+        self.nparam = param_count()
+
+    def close(self):
+        if self._n:
+            lib().bm_net_destroy(self._n)
+            self._n = ctypes.c_void_p(None)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._n
+
+    def params(self):
+        out = np.empty(self.nparam, np.float32)
+        check(lib().bm_net_get_params(self._n, out.ctypes.data, out.size))
+        return out
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        check(lib().bm_net_set_params(self._n, p.ctypes.data, p.size))
+
+    def save(self, path):
+        self.params().tofile(path)
+
+    def load(self, path):
+        self.set_params(np.fromfile(path, np.float32))
+
+    def prepare(self, b, d_f0, d_f1, W, H, stream=0):
+        check(lib().bm_net_prepare(self._n, b, ctypes.c_void_p(d_f0), ctypes.c_void_p(d_f1), W, H,
+                                   ctypes.c_void_p(stream)))
+
+    def set_input(self, d_in_bf16, B, h, w, stream=0):
+        check(lib().bm_net_set_input(self._n, ctypes.c_void_p(d_in_bf16), B, h, w, ctypes.c_void_p(stream)))
+
+    def forward(self, B, h, w, d_out=0, stream=0):
+        check(lib().bm_net_forward(self._n, B, h, w, ctypes.c_void_p(d_out), ctypes.c_void_p(stream)))
+
+    def train_step(self, B, h, w, d_target, lr, d_grad=0, stream=0):
+        loss = np.zeros(3, np.float32)
+        check(lib().bm_net_train_step(self._n, B, h, w, ctypes.c_void_p(d_target), lr, ctypes.c_void_p(d_grad),
+                                      loss.ctypes.data, ctypes.c_void_p(stream)))
+        return loss

@@ -246,6 +246,32 @@ bm_status bm_batch_autotune(bm_batch* b, const char* cache_path, int reps, char*
  * every block gives up, *timed_out is set and BM_ERR_TIMEOUT returned. */
 bm_status bm_selftest_barrier(uint32_t blocks, uint32_t expect, uint64_t spin_limit, int* timed_out);
 
+/* ---- learned flow proposal ---------------------------------------------------------- */
+
+/* No counterpart in the reference.  A 6-layer 3x3 convolutional network (2->32, 4x
+ * 32->32, 32->3; ReLU between) on the two frames at quarter resolution, BF16 weights
+ * and activations with FP32 accumulation on the tensor cores, predicting the flow
+ * (quarter-resolution pixels) and a confidence logit per quarter-resolution pixel.
+ * Parameters are one FP32 vector: for each layer W[cout][9][cin] then b[cout]. */
+typedef struct bm_net bm_net;
+size_t bm_net_param_count(void);
+bm_status bm_net_create(uint32_t max_batch, uint32_t max_h4, uint32_t max_w4, bm_net** out);
+bm_status bm_net_destroy(bm_net* n);
+bm_status bm_net_set_params(bm_net* n, const float* h_params, size_t count);
+bm_status bm_net_get_params(bm_net* n, float* h_params, size_t count);
+/* Input image b from two 8-bit W x H device frames (4x4 box average, [-1, 1]). */
+bm_status bm_net_prepare(bm_net* n, uint32_t b, const uint8_t* d_f0, const uint8_t* d_f1, uint32_t W, uint32_t H,
+                         void* stream);
+/* Raw input: B images h x w, bf16 NHWC with 16 channels (channels 0,1 used). */
+bm_status bm_net_set_input(bm_net* n, const uint16_t* d_in, uint32_t B, uint32_t h, uint32_t w, void* stream);
+/* Forward; d_out (may be NULL) receives [B][h][w][3] floats (u, v, confidence logit). */
+bm_status bm_net_forward(bm_net* n, uint32_t B, uint32_t h, uint32_t w, float* d_out, void* stream);
+/* Forward + loss against d_target ([B][h][w][3]: u, v, validity) + backward; with
+ * lr > 0 also one Adam step.  d_grad_out (may be NULL) receives the FP32 gradient;
+ * h_loss (may be NULL) receives (flow loss, confidence loss, confident fraction). */
+bm_status bm_net_train_step(bm_net* n, uint32_t B, uint32_t h, uint32_t w, const float* d_target, float lr,
+                            float* d_grad_out, float* h_loss, void* stream);
+
 /* ---- refinement without allocation ------------------------------------------------ */
 
 /* No counterpart in the reference.  The refinement of bm_process (median filter

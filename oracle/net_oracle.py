@@ -1,0 +1,107 @@
+"""FP32 CPU restatement of the proposal network's forward and backward passes
+(TEST INFRASTRUCTURE, the checker of the tensor-core kernels).
+
+It rounds to BF16 exactly where the GPU stores BF16 (weights, the network input,
+every ReLU activation, every activation gradient), so that the GPU and this
+restatement differ only by the order of FP32 accumulation.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+CIN = [2, 32, 32, 32, 32, 32]
+COUT = [32, 32, 32, 32, 32, 3]
+
+
+def bf16(x):
+    """Round float32 to the nearest bfloat16 (ties to even), returned as float32."""
+    a = np.ascontiguousarray(x, np.float32).view(np.uint32).astype(np.uint64)
+    r = ((a + 0x7FFF + ((a >> 16) & 1)) >> 16) << 16
+    return r.astype(np.uint32).view(np.float32).reshape(np.shape(x))
+
+
+def unpack(params):
+    out, k = [], 0
+    for ci, co in zip(CIN, COUT):
+        nw = co * 9 * ci
+        W = params[k:k + nw].reshape(co, 9, ci)
+        b = params[k + nw:k + nw + co]
+        out.append((W, b))
+        k += nw + co
+    assert k == params.size
+    return out
+
+
+def _shifts(x):
+    """The 9 zero-padded 3x3 neighbours of NHWC x: list of [B,h,w,C] (tap = dy*3+dx)."""
+    B, h, w, C = x.shape
+    p = np.zeros((B, h + 2, w + 2, C), np.float32)
+    p[:, 1:-1, 1:-1] = x
+    return [p[:, dy:dy + h, dx:dx + w] for dy in range(3) for dx in range(3)]
+
+
+def conv(x, W, b=None):
+    sh = _shifts(x)
+    y = sum(np.einsum("bhwc,oc->bhwo", sh[t], W[:, t, :], optimize=True) for t in range(9))
+    return y + (b if b is not None else 0)
+
+
+def _r(x, rounding):
+    return bf16(x) if rounding else np.asarray(x, np.float32)
+
+
+def forward(params, x0, rounding=True):
+    layers = unpack(params)
+    acts = []
+    x = _r(x0, rounding)
+    for l in range(5):
+        W, b = layers[l]
+        x = _r(np.maximum(conv(x, _r(W, rounding), b), 0), rounding)
+        acts.append(x)
+    W, b = layers[5]
+    return conv(x, _r(W, rounding), b).astype(np.float32), acts
+
+
+def loss_grad(out, target, tau=1.0, wconf=0.25, rounding=True):
+    n = out.shape[0] * out.shape[1] * out.shape[2]
+    u, v, c = out[..., 0], out[..., 1], out[..., 2]
+    tu, tv, valid = target[..., 0], target[..., 1], target[..., 2]
+    du, dv = u - tu, v - tv
+
+    def sl1(d):
+        a = np.abs(d)
+        return np.where(a < 1, 0.5 * d * d, a - 0.5), np.where(a < 1, d, np.sign(d))
+
+    lu, gu = sl1(du)
+    lv, gv = sl1(dv)
+    label = ((np.abs(du) + np.abs(dv)) < tau).astype(np.float32)
+    sig = 1 / (1 + np.exp(-c))
+    lc = valid * (np.maximum(c, 0) - c * label + np.log1p(np.exp(-np.abs(c))))
+    dY = np.zeros(out.shape[:3] + (3,), np.float32)
+    dY[..., 0] = gu * valid / n
+    dY[..., 1] = gv * valid / n
+    dY[..., 2] = wconf * (sig - label) * valid / n
+    losses = (float(((lu + lv) * valid).sum() / n), float(lc.sum() / n), float((valid * label).sum() / n))
+    return _r(dY, rounding), losses
+
+
+def backward(params, x0, acts, dY, rounding=True):
+    """FP32 gradient vector (same layout as params)."""
+    layers = unpack(params)
+    grads = []
+    xs = [_r(x0, rounding)] + acts
+    for l in range(5, -1, -1):
+        W, _ = layers[l]
+        X = xs[l]
+        sh = _shifts(X)
+        dW = np.stack([np.einsum("bhwo,bhwc->oc", dY, sh[t], optimize=True) for t in range(9)], axis=1)
+        db = dY.sum(axis=(0, 1, 2))
+        grads.append((dW, db))
+        if l > 0:
+            # dX[q] = sum_t dY[q - off(t)] W[:, t, :]: correlation with the flipped kernel
+            Wf = _r(W, rounding)[:, ::-1, :]
+            shd = _shifts(dY)
+            dX = sum(np.einsum("bhwo,oc->bhwc", shd[t], Wf[:, t, :], optimize=True) for t in range(9))
+            dY = _r(dX * (acts[l - 1] > 0), rounding)
+    grads = grads[::-1]
+    return np.concatenate([np.concatenate([dW.ravel(), db]) for dW, db in grads]).astype(np.float32)

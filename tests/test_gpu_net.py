@@ -1,0 +1,85 @@
+"""The proposal network's tensor-core kernels against the FP32 CPU restatement
+(oracle/net_oracle.py): forward output, loss terms and every layer's gradient."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from oracle import net_oracle
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("no GPU", allow_module_level=True)
+
+from briefmatch_gb300.proposal import ProposalNet, param_count  # noqa: E402
+
+
+def _bf16_bits(x):
+    a = np.ascontiguousarray(x, np.float32).view(np.uint32).astype(np.uint64)
+    return (((a + 0x7FFF + ((a >> 16) & 1)) >> 16) & 0xFFFF).astype(np.uint16)
+
+
+def _setup(B=2, h=20, w=36, seed=0):
+    rng = np.random.default_rng(seed)
+    net = ProposalNet(B, h, w)
+    p = net.params()
+    p += rng.normal(0, 0.02, p.size).astype(np.float32)  # non-zero biases too
+    net.set_params(p)
+    x = np.zeros((B, h, w, 16), np.float32)
+    x[..., :2] = rng.uniform(-1, 1, (B, h, w, 2))
+    d_in = torch.from_numpy(_bf16_bits(x).view(np.int16)).cuda()
+    net.set_input(d_in.data_ptr(), B, h, w)
+    tgt = np.zeros((B, h, w, 3), np.float32)
+    tgt[..., 0] = rng.normal(0, 1.5, (B, h, w))
+    tgt[..., 1] = rng.normal(0, 1.5, (B, h, w))
+    tgt[..., 2] = (rng.uniform(size=(B, h, w)) > 0.1).astype(np.float32)
+    return net, p, x[..., :2], tgt
+
+
+def test_param_count():
+    assert param_count() == 2 * 9 * 32 + 32 + 4 * (32 * 9 * 32 + 32) + 3 * 9 * 32 + 3
+
+
+def test_forward_matches_oracle():
+    B, h, w = 2, 20, 36
+    net, p, x, _ = _setup(B, h, w)
+    out = torch.empty(B, h, w, 3, device="cuda")
+    net.forward(B, h, w, out.data_ptr())
+    torch.cuda.synchronize()
+    got = out.cpu().numpy()
+    want, _ = net_oracle.forward(p, x)
+    err = np.abs(got - want).max() / max(1e-6, np.abs(want).max())
+    assert err < 2e-2, err
+
+
+def test_gradients_match_oracle():
+    B, h, w = 2, 20, 36
+    net, p, x, tgt = _setup(B, h, w, seed=1)
+    d_t = torch.from_numpy(tgt).cuda()
+    d_g = torch.empty(param_count(), device="cuda")
+    loss = net.train_step(B, h, w, d_t.data_ptr(), 0.0, d_g.data_ptr())
+    torch.cuda.synchronize()
+    got = d_g.cpu().numpy()
+    out, acts = net_oracle.forward(p, x)
+    dY, losses = net_oracle.loss_grad(out, tgt)
+    want = net_oracle.backward(p, x, acts, dY)
+    assert np.allclose(loss, losses, rtol=2e-2, atol=1e-5), (loss, losses)
+    k = 0
+    for l, (ci, co) in enumerate(zip(net_oracle.CIN, net_oracle.COUT)):
+        n = co * 9 * ci + co
+        g, wv = got[k:k + n], want[k:k + n]
+        rel = np.linalg.norm(g - wv) / max(1e-12, np.linalg.norm(wv))
+        assert rel < 3e-2, (l, rel)
+        k += n
+
+
+def test_training_reduces_loss():
+    B, h, w = 4, 24, 32
+    net, p, x, tgt = _setup(B, h, w, seed=2)
+    d_t = torch.from_numpy(tgt).cuda()
+    first = net.train_step(B, h, w, d_t.data_ptr(), 1e-3)
+    for _ in range(60):
+        last = net.train_step(B, h, w, d_t.data_ptr(), 1e-3)
+    assert last[0] < 0.8 * first[0]
