@@ -103,6 +103,8 @@ def _declare(lib):
         "bm_profile_enable": (c.c_int, [c.c_void_p, c.c_int]),
         "bm_profile_reset": (c.c_int, [c.c_void_p]),
         "bm_profile_read": (c.c_int, [c.c_void_p, c.c_void_p, c.c_uint32, P(c.c_uint32)]),
+        "bm_set_proposal": (c.c_int, [c.c_void_p, c.c_void_p, c.c_float, c.c_uint32, c.c_uint32]),
+        "bm_seed": (c.c_int, [c.c_void_p, c.c_int, c.c_void_p, c.c_uint32, c.c_uint32, c.c_float]),
         "bm_refine_noalloc": (c.c_int, [c.c_void_p, c.c_void_p, c.c_void_p, c.c_void_p, c.c_void_p, c.c_uint32,
                                         c.c_uint32, c.c_uint32, c.c_float, c.c_float, c.c_float, c.c_void_p]),
         "bm_refine_noalloc_max_pixels": (c.c_uint64, []),
@@ -488,6 +490,17 @@ class Batch:
 
     def launch_count(self):
         return int(lib().bm_batch_launch_count(self._b))
+
+
+def set_proposal(engine, net, conf_threshold=0.5, iterations=1, jf_max=16):
+    """Attach a ProposalNet (or None) to a BriefMatch context (bm_set_proposal)."""
+    check(lib().bm_set_proposal(engine.ctx, net.handle if net is not None else None, conf_threshold, iterations,
+                                jf_max))
+
+
+def seed(engine, first, d_pred, w4, h4, conf_threshold=0.5):
+    """Seeded initialisation from a [h4][w4][3] device prediction (bm_seed)."""
+    check(lib().bm_seed(engine.ctx, int(bool(first)), ctypes.c_void_p(d_pred), w4, h4, conf_threshold))
 
 
 def selftest_barrier(blocks, expect, spin_limit):

@@ -60,7 +60,7 @@ struct bm_ctx {
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
 
-    uint8_t* d_frame_u8 = nullptr;
+    uint8_t* d_u8[2] = {nullptr, nullptr};   // 8-bit frames, [cur_frame] current
     float* d_frame[2] = {nullptr, nullptr};  // [cur_frame] current, [cur_frame^1] previous
     int cur_frame = 0;
     float* d_up = nullptr;
@@ -91,6 +91,12 @@ struct bm_ctx {
     bool first_match = true; // BriefMatch::m_firstFrame
     bool primed = false;
     uint64_t launches = 0;
+
+    // learned proposal (bm_set_proposal)
+    bm_net* net = nullptr;
+    float net_logit_min = 0.0f;
+    uint32_t net_iterations = 0, net_jfMax = 0;
+    float* d_pred = nullptr;   // [h4][w4][3]
 
     struct ProfRec {
         const char* name;
@@ -177,7 +183,7 @@ bm_status dev_alloc(T** p, size_t count)
 
 void release(bm_ctx* c)
 {
-    void* ptrs[] = {c->d_frame_u8, c->d_frame[0], c->d_frame[1], c->d_up, c->d_feat[0], c->d_feat[1],
+    void* ptrs[] = {c->d_u8[0], c->d_u8[1], c->d_pred, c->d_frame[0], c->d_frame[1], c->d_up, c->d_feat[0], c->d_feat[1],
                     c->d_flow[0], c->d_flow[1], c->d_cost, c->d_flow_in, c->d_flow_med, c->d_flow_out,
                     c->d_tmp, c->d_pattern, c->d_taps, c->d_lx, c->d_ix, c->d_ly, c->d_iy,
                     c->d_nnx, c->d_nny};
@@ -225,13 +231,13 @@ bm_status features_into(bm_ctx* c, const float* d_up, uint32_t* F)
 
 // One jump-flood pass; the random search of this iteration is fused into the last
 // level when fuse_rs is set (it reads only the pixel's own state).
-bm_status propagate_pass(bm_ctx* c, int pd, bool fuse_rs)
+bm_status propagate_pass(bm_ctx* c, int pd, bool fuse_rs, uint32_t jfMax)
 {
     const bm_params& p = c->prm;
     int levels = 0;
-    for (int step = (int)p.jfMax; step > 0; step /= 2) levels++;
+    for (int step = (int)jfMax; step > 0; step /= 2) levels++;
     int lvl = 0;
-    for (int step = (int)p.jfMax; step > 0; step /= 2, lvl++) {
+    for (int step = (int)jfMax; step > 0; step /= 2, lvl++) {
         const bool last = (lvl == levels - 1);
         bmk::RsArgs rs = rs_args(c, fuse_rs && last);
         BM_LAUNCH(c, rs.enabled ? "jump_level_rs" : "jump_level", bmk::jump_level(c->feat1_ptr(), c->feat2_ptr(), c->d_flow[c->flow_cur], c->d_flow[c->flow_cur ^ 1],
@@ -250,18 +256,32 @@ bm_status propagate_pass(bm_ctx* c, int pd, bool fuse_rs)
     return BM_OK;
 }
 
-bm_status match_impl(bm_ctx* c, const float* d_im2)
+// BriefMatch::match.  With a proposal network attached (and its prediction in
+// d_pred), the initialisation is the seeded one and the iteration count and jump
+// maximum are the proposal's.
+bm_status match_impl(bm_ctx* c, const float* d_im2, bool seeded)
 {
     const bm_params& p = c->prm;
     bm_status st = features_into(c, d_im2, c->feat2_ptr());
     if (st != BM_OK) return st;
     const int first = (c->first_match || !p.tInit) ? 1 : 0;
-    BM_LAUNCH(c, "initialize", bmk::initialize(c->feat1_ptr(), c->feat2_ptr(), c->d_flow[c->flow_cur], c->d_flow[c->flow_cur ^ 1],
-                                 c->d_cost, (int)p.sx, (int)p.sy, (int)c->nsp, first, next_order(c), c->stream));
+    uint32_t iterations = p.iterations, jfMax = p.jfMax;
+    if (seeded) {
+        const int w4 = (int)p.sx_in / 4, h4 = (int)p.sy_in / 4;
+        const float scx = 4.0f * (float)p.sx / (float)p.sx_in, scy = 4.0f * (float)p.sy / (float)p.sy_in;
+        BM_LAUNCH(c, "seed", bmk::seed_field(c->feat1_ptr(), c->feat2_ptr(), c->d_flow[c->flow_cur], c->d_flow[c->flow_cur ^ 1],
+                                             c->d_cost, (int)p.sx, (int)p.sy, (int)c->nsp, first, c->d_pred, w4, h4, scx,
+                                             scy, c->net_logit_min, c->stream));
+        iterations = c->net_iterations;
+        if (c->net_jfMax) jfMax = c->net_jfMax;
+    } else {
+        BM_LAUNCH(c, "initialize", bmk::initialize(c->feat1_ptr(), c->feat2_ptr(), c->d_flow[c->flow_cur], c->d_flow[c->flow_cur ^ 1],
+                                     c->d_cost, (int)p.sx, (int)p.sy, (int)c->nsp, first, next_order(c), c->stream));
+    }
     c->flow_cur ^= 1;
     int pd = -1;
-    for (uint32_t it = 0; it < p.iterations; it++) {
-        st = propagate_pass(c, pd, true);
+    for (uint32_t it = 0; it < iterations; it++) {
+        st = propagate_pass(c, pd, true, jfMax);
         if (st != BM_OK) return st;
         pd = -pd;
     }
@@ -396,7 +416,9 @@ bm_status bm_create(const bm_params* prm, bm_ctx** out)
     }
     c->stream = c->own_stream;
     const size_t n = c->npix, ni = c->npix_in;
-    BM_TRY(dev_alloc(&c->d_frame_u8, ni));
+    BM_TRY(dev_alloc(&c->d_u8[0], ni));
+    BM_TRY(dev_alloc(&c->d_u8[1], ni));
+    BM_TRY(dev_alloc(&c->d_pred, (size_t)(p.sx_in / 4 + 1) * (p.sy_in / 4 + 1) * 3));
     BM_TRY(dev_alloc(&c->d_frame[0], ni));
     BM_TRY(dev_alloc(&c->d_frame[1], ni));
     BM_TRY(dev_alloc(&c->d_up, n));
@@ -589,7 +611,7 @@ bm_status bm_initialize(bm_ctx* c, int first)
 bm_status bm_propagate(bm_ctx* c, int pd)
 {
     if (check_ctx(c)) return BM_ERR_INVALID;
-    return propagate_pass(c, pd, false);
+    return propagate_pass(c, pd, false, c->prm.jfMax);
 }
 
 bm_status bm_random_search(bm_ctx* c)
@@ -608,7 +630,7 @@ bm_status bm_match(bm_ctx* c, const float* d_im1, const float* d_im2)
     (void)d_im1;
     if (check_ctx(c)) return BM_ERR_INVALID;
     if (!d_im2) return fail(BM_ERR_INVALID, "bm_match: null frame");
-    return match_impl(c, d_im2);
+    return match_impl(c, d_im2, false);
 }
 
 bm_status bm_downsample(bm_ctx* c)
@@ -691,6 +713,35 @@ bm_status bm_set_rng_position(bm_ctx* c, uint64_t calls)
     return BM_OK;
 }
 
+bm_status bm_set_proposal(bm_ctx* c, bm_net* net, float conf_threshold, uint32_t iterations, uint32_t jfMax)
+{
+    if (check_ctx(c)) return BM_ERR_INVALID;
+    if (net && !(conf_threshold > 0.0f && conf_threshold < 1.0f))
+        return fail(BM_ERR_INVALID, "bm_set_proposal: confidence threshold must lie in (0, 1)");
+    if (net && (c->prm.sx_in < 4 || c->prm.sy_in < 4)) return fail(BM_ERR_LIMIT, "bm_set_proposal: frame too small");
+    c->net = net;
+    c->net_logit_min = net ? std::log(conf_threshold / (1.0f - conf_threshold)) : 0.0f;
+    c->net_iterations = iterations;
+    c->net_jfMax = jfMax;
+    return BM_OK;
+}
+
+bm_status bm_seed(bm_ctx* c, int first, const float* d_pred, uint32_t w4, uint32_t h4, float conf_threshold)
+{
+    if (check_ctx(c)) return BM_ERR_INVALID;
+    if (!d_pred || w4 == 0 || h4 == 0) return fail(BM_ERR_INVALID, "bm_seed: bad prediction");
+    if (!(conf_threshold > 0.0f && conf_threshold < 1.0f))
+        return fail(BM_ERR_INVALID, "bm_seed: confidence threshold must lie in (0, 1)");
+    const bm_params& p = c->prm;
+    const float scx = (float)p.sx / (float)w4, scy = (float)p.sy / (float)h4;
+    BM_LAUNCH(c, "seed", bmk::seed_field(c->feat1_ptr(), c->feat2_ptr(), c->d_flow[c->flow_cur], c->d_flow[c->flow_cur ^ 1],
+                                         c->d_cost, (int)p.sx, (int)p.sy, (int)c->nsp, first ? 1 : 0, d_pred, (int)w4,
+                                         (int)h4, scx, scy, std::log(conf_threshold / (1.0f - conf_threshold)),
+                                         c->stream));
+    c->flow_cur ^= 1;
+    return BM_OK;
+}
+
 bm_status bm_reset_sequence(bm_ctx* c)
 {
     if (check_ctx(c)) return BM_ERR_INVALID;
@@ -737,12 +788,11 @@ bm_status bm_frame(bm_ctx* c, const uint8_t* frame, int frame_on_device, float* 
     if (!frame) return fail(BM_ERR_INVALID, "bm_frame: null frame");
     const bm_params& p = c->prm;
     const size_t ni = c->npix_in;
-    const uint8_t* d_u8 = frame;
-    if (!frame_on_device) {
-        // of_pipeline.cpp:297 (8-bit here: a quarter of the reference's float copy)
-        BM_CUDA(cudaMemcpyAsync(c->d_frame_u8, frame, ni, cudaMemcpyHostToDevice, c->stream));
-        d_u8 = c->d_frame_u8;
-    }
+    // of_pipeline.cpp:297 (8-bit here: a quarter of the reference's float copy); the
+    // frame is kept for the next pair's proposal input
+    uint8_t* d_u8 = c->d_u8[c->cur_frame];
+    BM_CUDA(cudaMemcpyAsync(d_u8, frame, ni, frame_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                            c->stream));
     float* cur = c->d_frame[c->cur_frame];
     BM_LAUNCH(c, "u8_to_f32", bmk::u8_to_f32(d_u8, cur, ni, c->stream));
     // of_pipeline.cpp:301-310
@@ -759,7 +809,15 @@ bm_status bm_frame(bm_ctx* c, const uint8_t* frame, int frame_on_device, float* 
         BM_CUDA(cudaMemsetAsync(c->d_flow_out, 0, 2 * ni * sizeof(float), c->stream));
         c->primed = true;
     } else {
-        st = match_impl(c, up);                                   // of_pipeline.cpp:314
+        const bool seeded = c->net != nullptr;
+        if (seeded) {
+            const uint32_t w4 = p.sx_in / 4, h4 = p.sy_in / 4;
+            st = bm_net_prepare(c->net, 0, c->d_u8[c->cur_frame ^ 1], d_u8, p.sx_in, p.sy_in, c->stream);
+            if (st == BM_OK) st = bm_net_forward(c->net, 1, h4, w4, c->d_pred, c->stream);
+            if (st != BM_OK) return st;
+            c->launches += 7;
+        }
+        st = match_impl(c, up, seeded);                           // of_pipeline.cpp:314
         if (st == BM_OK) st = downsample_impl(c);                 // :319
         if (st == BM_OK) st = process_impl(c, c->d_frame[c->cur_frame ^ 1]);  // :324
         if (st != BM_OK) return st;

@@ -276,6 +276,53 @@ __device__ __forceinline__ void init_px(const uint32_t* __restrict__ F1, const u
     flow_out[pix] = pack_flow(nx, ny);
 }
 
+// Seeded initialisation: first the plain initialisation (zero vector, or the
+// temporal candidate when !first, exactly as init_px), then the network's proposal
+// for this pixel -- pred is [h4][w4][3] (u, v in quarter-resolution input pixels,
+// confidence logit) -- where its confidence logit reaches logit_min; the proposal
+// replaces the plain vector only if its Hamming cost is strictly lower.
+template <int NSP>
+__device__ __forceinline__ void seed_px(const uint32_t* __restrict__ F1, const uint32_t* __restrict__ F2,
+                                        const uint32_t* __restrict__ flow_prev, uint32_t* __restrict__ flow_out,
+                                        uint16_t* __restrict__ cost, int sx, int sy, int first, int x, int y,
+                                        const float* __restrict__ pred, int w4, int h4, float scale_x, float scale_y,
+                                        float inv_x, float inv_y, float logit_min)
+{
+    const long n = (long)sx * sy;
+    const long pix = x + (long)y * sx;
+    int nx = 0, ny = 0;
+    if (!first) {
+        uint32_t own = flow_prev[pix];
+        long q = pix + lo16(own) + (long)hi16(own) * sx;
+        uint32_t t = (q >= 0 && q < n) ? flow_prev[q] : 0u;
+        nx = min(max(lo16(t), -x), sx - x - 1);
+        ny = min(max(hi16(t), -y), sy - y - 1);
+    }
+    uint32_t f1[NSP];
+    load_desc<NSP>(f1, F1 + pix * NSP);
+    int h = hamming<NSP>(f1, F2 + (pix + nx + (long)ny * sx) * NSP);
+    // quarter-resolution cell of this up-sampled pixel (scale = up-sampled px per
+    // quarter-resolution px, inv = its reciprocal from the host, so the cell index
+    // is one IEEE add and multiply: no approximate division)
+    const int qx = min(w4 - 1, max(0, (int)((x + 0.5f) * inv_x)));
+    const int qy = min(h4 - 1, max(0, (int)((y + 0.5f) * inv_y)));
+    const float* pr = pred + ((size_t)qy * w4 + qx) * 3;
+    if (pr[2] >= logit_min) {
+        const int sxv = min(max(__float2int_rn(pr[0] * scale_x), -x), sx - x - 1);
+        const int syv = min(max(__float2int_rn(pr[1] * scale_y), -y), sy - y - 1);
+        if (sxv != nx || syv != ny) {
+            const int hs = hamming<NSP>(f1, F2 + (pix + sxv + (long)syv * sx) * NSP);
+            if (hs < h) {
+                h = hs;
+                nx = sxv;
+                ny = syv;
+            }
+        }
+    }
+    cost[pix] = (uint16_t)h;
+    flow_out[pix] = pack_flow(nx, ny);
+}
+
 // One jump-flood level at step p (briefmatch_cuda.cu:206-219) for pixel (x, y).
 // Neighbours are read from flow_in (the previous level's field) and the result is
 // written to flow_out, so the outcome does not depend on the schedule.  All

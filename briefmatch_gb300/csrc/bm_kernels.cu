@@ -106,6 +106,19 @@ __global__ void __launch_bounds__(256) k_initialize(const uint32_t* __restrict__
     init_px<NSP>(F1, F2, flow_prev, flow_out, cost, sx, sy, first, x, y);
 }
 
+template <int NSP>
+__global__ void __launch_bounds__(256) k_seed(const uint32_t* __restrict__ F1, const uint32_t* __restrict__ F2,
+                                              const uint32_t* __restrict__ flow_prev, uint32_t* __restrict__ flow_out,
+                                              uint16_t* __restrict__ cost, int sx, int sy, int first,
+                                              const float* __restrict__ pred, int w4, int h4, float scale_x,
+                                              float scale_y, float inv_x, float inv_y, float logit_min)
+{
+    const int x = blockIdx.x * TX + threadIdx.x, y = blockIdx.y * TY + threadIdx.y;
+    if (x >= sx || y >= sy) return;
+    seed_px<NSP>(F1, F2, flow_prev, flow_out, cost, sx, sy, first, x, y, pred, w4, h4, scale_x, scale_y, inv_x, inv_y,
+                 logit_min);
+}
+
 template <int NSP, bool RS>
 __global__ void __launch_bounds__(256) k_jump_level(const uint32_t* __restrict__ F1, const uint32_t* __restrict__ F2,
                                                     const uint32_t* __restrict__ flow_in, uint32_t* __restrict__ flow_out,
@@ -318,6 +331,16 @@ cudaError_t initialize(const uint32_t* F1, const uint32_t* F2, const uint32_t* f
                        cudaStream_t st)
 {
     BM_DISPATCH_NSP(nsp, k_initialize<NSP><<<grid2d(sx, sy), dim3(TX, TY), 0, st>>>(F1, F2, flow_prev, flow_out, cost, sx, sy, first, rev));
+    return cudaGetLastError();
+}
+
+cudaError_t seed_field(const uint32_t* F1, const uint32_t* F2, const uint32_t* flow_prev, uint32_t* flow_out,
+                       uint16_t* cost, int sx, int sy, int nsp, int first, const float* pred, int w4, int h4,
+                       float scale_x, float scale_y, float logit_min, cudaStream_t st)
+{
+    // host IEEE reciprocals: the device cell lookup multiplies by them
+    const float inv_x = 1.0f / scale_x, inv_y = 1.0f / scale_y;
+    BM_DISPATCH_NSP(nsp, k_seed<NSP><<<grid2d(sx, sy), dim3(TX, TY), 0, st>>>(F1, F2, flow_prev, flow_out, cost, sx, sy, first, pred, w4, h4, scale_x, scale_y, inv_x, inv_y, logit_min));
     return cudaGetLastError();
 }
 

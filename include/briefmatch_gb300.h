@@ -272,6 +272,20 @@ bm_status bm_net_forward(bm_net* n, uint32_t B, uint32_t h, uint32_t w, float* d
 bm_status bm_net_train_step(bm_net* n, uint32_t B, uint32_t h, uint32_t w, const float* d_target, float lr,
                             float* d_grad_out, float* h_loss, void* stream);
 
+/* Attach a proposal network to a context (NULL detaches).  Every later bm_frame that
+ * matches a pair runs the network on the previous and current frames and initialises
+ * matching by bm_seed's rule, then runs `iterations` rounds with jump-flood maximum
+ * jfMax (0 keeps the context's).  The network must have been created for at least
+ * one image of (sx_in/4) x (sy_in/4). */
+bm_status bm_set_proposal(bm_ctx* ctx, bm_net* net, float conf_threshold, uint32_t iterations, uint32_t jfMax);
+
+/* Seeded initialisation (the stage entry point): each up-sampled pixel first takes
+ * the plain initialisation (CUDA_initialize semantics: zero vector, or the temporal
+ * candidate when first == 0), then the prediction's vector of its w4 x h4 cell
+ * (d_pred [h4][w4][3]: u, v in cell units, confidence logit) where the confidence
+ * reaches conf_threshold -- kept only if its Hamming cost is strictly lower. */
+bm_status bm_seed(bm_ctx* ctx, int first, const float* d_pred, uint32_t w4, uint32_t h4, float conf_threshold);
+
 /* ---- refinement without allocation ------------------------------------------------ */
 
 /* No counterpart in the reference.  The refinement of bm_process (median filter

@@ -98,6 +98,44 @@ def initialize(F1, F2, sx, sy, N, first, NX=None, NY=None):
     return NX, NY, H
 
 
+def _hamming_rows(A, B):
+    x = np.ascontiguousarray(A ^ B)
+    return np.unpackbits(x.view(np.uint8), axis=1).sum(axis=1).astype(np.int64)
+
+
+def seed(F1, F2, sx, sy, N, first, pred, w4, h4, scale_x, scale_y, logit_min, NX=None, NY=None):
+    """Initialisation seeded by a quarter-resolution proposal [h4][w4][3] (u, v in
+    quarter-resolution pixels, confidence logit).  No reference counterpart: the
+    plain initialisation (briefmatch_cuda.cu:115-139 via bmo_initialize) runs first,
+    then each pixel whose cell has logit >= logit_min tries the proposal vector
+    (scaled by scale_x/y, rounded half-to-even, clamped into the image) and keeps it
+    only when its Hamming cost is strictly lower.  The cell of up-sampled pixel x is
+    floor((x + 0.5) * (1 / scale_x)) in float32, clamped to the grid."""
+    NX, NY, H = initialize(F1, F2, sx, sy, N, first, NX, NY)
+    F1 = _c(F1, np.uint32)
+    F2 = _c(F2, np.uint32)
+    f32 = np.float32
+    ys, xs = np.mgrid[0:sy, 0:sx]
+    xs, ys = xs.ravel(), ys.ravel()
+    inv_x, inv_y = f32(1.0) / f32(scale_x), f32(1.0) / f32(scale_y)
+    qx = np.clip(((xs.astype(f32) + f32(0.5)) * inv_x).astype(np.int64), 0, w4 - 1)
+    qy = np.clip(((ys.astype(f32) + f32(0.5)) * inv_y).astype(np.int64), 0, h4 - 1)
+    pr = np.asarray(pred, f32).reshape(h4, w4, 3)[qy, qx]
+    cand = pr[:, 2] >= f32(logit_min)
+    sxv = np.clip(np.rint(pr[:, 0] * f32(scale_x)).astype(np.int64), -xs, sx - xs - 1)
+    syv = np.clip(np.rint(pr[:, 1] * f32(scale_y)).astype(np.int64), -ys, sy - ys - 1)
+    cand &= (sxv != NX) | (syv != NY)
+    idx = np.nonzero(cand)[0]
+    q = idx + sxv[idx] + syv[idx] * sx
+    hs = _hamming_rows(F1[idx], F2[q])
+    win = hs < H[idx].astype(np.int64)
+    w = idx[win]
+    NX[w] = sxv[w]
+    NY[w] = syv[w]
+    H[w] = hs[win]
+    return NX, NY, H
+
+
 def jump_level(F1, F2, sx, sy, N, p, pd, double_prop, NX, NY, H):
     NXs = _c(NX, np.int16).copy()
     NYs = _c(NY, np.int16).copy()
@@ -206,9 +244,16 @@ class Sequence:
     ``up_images`` lets a caller supply the up-sampled frames (e.g. the engine's,
     to take libm-vs-fast-math Lanczos differences out of a comparison);
     ``normals_fn(call, n)`` supplies the random-search normals of call ``call``;
-    ``nn`` the device's down-sampling index tables (see ``downsample``)."""
+    ``nn`` the device's down-sampling index tables (see ``downsample``).
+    ``proposal`` = (pred_fn, logit_min, iterations, jf_max) switches matching to
+    the seeded schedule: pred_fn(prev_u8, cur_u8) gives the [h4][w4][3]
+    quarter-resolution proposal, ``seed`` replaces the plain initialisation and
+    the proposal's iteration count and jump maximum replace the parameters'
+    (jf_max 0 keeps them)."""
 
-    def __init__(self, params: dict, pattern, normals_fn, nn=None):
+    def __init__(self, params: dict, pattern, normals_fn, nn=None, proposal=None):
+        self.proposal = proposal
+        self.prev_u8 = None
         self.p = dict(params)
         self.nn = nn
         self.pattern = np.ascontiguousarray(pattern, np.float32)
@@ -234,8 +279,25 @@ class Sequence:
             nrm = np.concatenate([np.asarray(self.normals_fn(self.calls + k, n), np.float32).ravel() for k in range(it)]) \
                 if it else np.zeros(2 * n, np.float32)
             first = self.first or not p["tInit"]
-            NX, NY, H = match(self.F1, F2, sx, sy, N, it, p["jfMax"], p["doubleProp"], first, search_dist(sx), nrm,
-                              self.NX, self.NY)
+            if self.proposal is None:
+                NX, NY, H = match(self.F1, F2, sx, sy, N, it, p["jfMax"], p["doubleProp"], first, search_dist(sx), nrm,
+                                  self.NX, self.NY)
+            else:
+                pred_fn, logit_min, it, jf = self.proposal
+                jf = jf or p["jfMax"]
+                w4, h4 = sxi // 4, syi // 4
+                f32 = np.float32
+                scx = f32(4.0) * f32(sx) / f32(sxi)
+                scy = f32(4.0) * f32(sy) / f32(syi)
+                pred = pred_fn(self.prev_u8, frame_u8)
+                NX, NY, H = seed(self.F1, F2, sx, sy, N, first, pred, w4, h4, scx, scy, logit_min, self.NX, self.NY)
+                pd = -1
+                for k in range(it):
+                    NX, NY, H = propagate(self.F1, F2, sx, sy, N, pd, jf, p["doubleProp"], NX, NY, H)
+                    NX, NY, H = random_search(self.F1, F2, sx, sy, N, search_dist(sx),
+                                              np.asarray(self.normals_fn(self.calls + k, n), np.float32).ravel(),
+                                              NX, NY, H)
+                    pd = -pd
             self.calls += it
             self.first = False
             self.NX, self.NY, self.H = NX, NY, H
@@ -249,4 +311,5 @@ class Sequence:
                 out = (U, V)
         self.F1 = F2
         self.prev_in = cur_in
+        self.prev_u8 = np.asarray(frame_u8)
         return out
