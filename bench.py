@@ -8,7 +8,13 @@ the reference's "moderate" setting.  Synthetic frames stand in for the public
 benchmark sequences.
 
   value    7 pairs * 1024*436 output pixels / device time per step (frames
-           already in HBM as uint8, outputs left in HBM); L2 flushed between steps
+           already in HBM as uint8, outputs left in HBM); L2 flushed between steps.
+           Two engines are measured: the plain engine (the reference's method and
+           schedule) and the learned-seeded engine (the trained proposal seeds
+           matching; its (iterations, jfMax) is the fastest whose EPE on a separate
+           calibration sequence is at most the plain engine's).  The headline is
+           the learned-seeded engine when its EPE on the measured sequence is at
+           most the plain engine's, else the plain engine; both are reported.
   e2e      the same through the public C ABI with pinned host frames in and host
            flow out (H2D and D2H inside the timed region)
   roofline the dominant kernel's algorithmic bytes per launch over its mean
@@ -43,7 +49,7 @@ METRIC = "output flow Mpx/s at fixed EPE: batched+learned-seeded vs plain, same 
 UNIT = "Mpx/s"
 W, H, FRAMES, UP, NBITS, VMAX, SEED = 1024, 436, 8, 2.9, 128, 15.0, 20261203
 PAIRS = FRAMES - 1
-WORKLOAD = ("plain engine, synthetic 1024x436 8-bit sequence of 8 frames (7 pairs, |v|<=15 px), "
+WORKLOAD = ("%s engine, synthetic 1024x436 8-bit sequence of 8 frames (7 pairs, |v|<=15 px), "
             "up-sampling 2.9x2.9, feature_length 128, temporal init, FP32 flow out")
 
 
@@ -57,6 +63,7 @@ def parse():
     ap.add_argument("--cpu-pairs", type=int, default=2, help="pairs in the CPU-baseline sample")
     ap.add_argument("--no-batched", action="store_true", help="skip the 64-pair batched workload")
     ap.add_argument("--batch-pairs", type=int, default=64)
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-seeded engine")
     return ap.parse_args()
 
 
@@ -189,44 +196,51 @@ def algorithmic_bytes(kernel, prm):
     return table.get(kernel)
 
 
-def run_engine(args, torch, world, rank):
-    import numpy as np
+PROPOSAL_CONF = 0.5
+SCHEDULE_CANDIDATES = ((1, 16), (1, 32), (1, 64), (1, 128), (1, 256), (2, 16), (2, 32), (2, 64))
 
+
+def open_engine(torch, prm, pattern, stream, net=None, schedule=None):
     import briefmatch_gb300 as bm
 
-    frames, flows = make_workload(rank)
-    batch_inputs = None if args.no_batched else make_batch_workload(args.batch_pairs)
-    prm = bm.BMParams.derive(W, H, UP, UP, N=NBITS)
     eng = bm.BriefMatch(prm)
     eng.setup()
-    pattern = prm.make_pattern(SEED)
     eng.set_pattern(pattern)
-    # one explicit (non-default) stream carries the engine's work, the L2 flush and
-    # the timing events
-    stream = torch.cuda.Stream()
     eng.set_stream(stream.cuda_stream)
-    torch.cuda.set_stream(stream)
+    if net is not None:
+        bm.set_proposal(eng, net, PROPOSAL_CONF, schedule[0], schedule[1])
+    return eng
 
-    d_frames = torch.from_numpy(np.stack(frames)).cuda()
-    d_u = torch.empty(PAIRS, H, W, device="cuda")
-    d_v = torch.empty(PAIRS, H, W, device="cuda")
-    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")  # > 129 MB L2
 
-    def step():
-        # every step is the same sequence from the same random-stream position
-        eng.reset_sequence()
-        eng.set_rng_position(0)
-        for k in range(FRAMES):
-            if k == 0:
-                eng.frame(d_frames[0].data_ptr(), True)
-            else:
-                eng.frame(d_frames[k].data_ptr(), True, d_u[k - 1].data_ptr(), d_v[k - 1].data_ptr(), True)
+def sequence_step(eng, frame_ptrs, u_ptrs, v_ptrs, on_device):
+    """One step: the whole sequence from the same random-stream position."""
+    eng.reset_sequence()
+    eng.set_rng_position(0)
+    eng.frame(frame_ptrs[0], on_device)
+    for k in range(1, len(frame_ptrs)):
+        eng.frame(frame_ptrs[k], on_device, u_ptrs[k - 1], v_ptrs[k - 1], on_device)
 
+
+def mean_epe(u, v, flows):
+    import numpy as np
+
+    return [float(np.mean(np.hypot(u[k] - flows[k][0], v[k] - flows[k][1]))) for k in range(len(flows))]
+
+
+def measure(args, torch, world, eng, d_frames, flows, stream, flush):
+    """Device throughput of one engine over the sequence: W warm-up steps, then K
+    steps timed with CUDA events on the engine stream, L2 flushed before each step
+    (outside the events), per-kernel CUDA-event profile and SM clocks sampled over
+    the timed region."""
+    npairs = d_frames.shape[0] - 1
+    d_u = torch.empty(npairs, H, W, device="cuda")
+    d_v = torch.empty(npairs, H, W, device="cuda")
+    fp = [d_frames[k].data_ptr() for k in range(npairs + 1)]
+    up = [d_u[k].data_ptr() for k in range(npairs)]
+    vp = [d_v[k].data_ptr() for k in range(npairs)]
     for _ in range(args.warmup):
-        step()
+        sequence_step(eng, fp, up, vp, True)
     torch.cuda.synchronize()
-
-    # timed region: per-step CUDA events; L2 flushed before every step, outside the events
     eng.profile(True)
     eng.profile_reset()
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
@@ -238,55 +252,137 @@ def run_engine(args, torch, world, rank):
         for i in range(args.steps):
             flush.zero_()
             starts[i].record(stream)
-            step()
+            sequence_step(eng, fp, up, vp, True)
             ends[i].record(stream)
         torch.cuda.synchronize()
         barrier(torch, world)
     launches = eng.launch_count() - launches0
-    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    total_ms = max_over_ranks(torch, world, sum(step_ms))
+    total_ms = max_over_ranks(torch, world, sum(s.elapsed_time(e) for s, e in zip(starts, ends)))
     kstats = eng.profile_read()
     eng.profile(False)
-    ms_per_step = total_ms / args.steps
-    px_step = PAIRS * W * H
-    value = world * px_step / (ms_per_step * 1e-3) / 1e6
+    ms = total_ms / args.steps
+    u, v = d_u.cpu().numpy(), d_v.cpu().numpy()
+    return {"ms_per_step": ms, "value": world * npairs * W * H / (ms * 1e-3) / 1e6, "launches": launches,
+            "kstats": kstats, "clocks": clk.summary(), "epe": mean_epe(u, v, flows), "u": u, "v": v}
 
-    # accuracy of the last step
-    u = d_u.cpu().numpy()
-    v = d_v.cpu().numpy()
-    epes = [float(np.mean(np.hypot(u[k] - flows[k][0], v[k] - flows[k][1]))) for k in range(PAIRS)]
 
-    # end to end through the C ABI with pinned host buffers
+def measure_e2e(args, torch, world, eng, frames, u_dev, v_dev, flush):
+    """The same step through the public C ABI with pinned host frames in and host
+    flow out: host-to-device and device-to-host copies inside the timed region."""
+    import numpy as np
+
+    npairs = len(frames) - 1
     h_frames = torch.from_numpy(np.stack(frames)).pin_memory()
-    h_u = torch.empty(PAIRS, H, W).pin_memory()
-    h_v = torch.empty(PAIRS, H, W).pin_memory()
-
-    def step_e2e():
-        eng.reset_sequence()
-        eng.set_rng_position(0)
-        for k in range(FRAMES):
-            if k == 0:
-                eng.frame(h_frames[0].data_ptr(), False)
-            else:
-                eng.frame(h_frames[k].data_ptr(), False, h_u[k - 1].data_ptr(), h_v[k - 1].data_ptr(), False)
-
+    h_u = torch.empty(npairs, H, W).pin_memory()
+    h_v = torch.empty(npairs, H, W).pin_memory()
+    fp = [h_frames[k].data_ptr() for k in range(npairs + 1)]
+    up = [h_u[k].data_ptr() for k in range(npairs)]
+    vp = [h_v[k].data_ptr() for k in range(npairs)]
     for _ in range(max(1, args.warmup)):
-        step_e2e()
+        sequence_step(eng, fp, up, vp, False)
     torch.cuda.synchronize()
     e2e_ms = 0.0
     barrier(torch, world)
-    for i in range(args.steps):
+    for _ in range(args.steps):
         flush.zero_()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        step_e2e()
+        sequence_step(eng, fp, up, vp, False)
         torch.cuda.synchronize()
         e2e_ms += (time.perf_counter() - t0) * 1e3
     e2e_ms = max_over_ranks(torch, world, e2e_ms)
-    e2e_value = world * px_step / (e2e_ms / args.steps * 1e-3) / 1e6
-    assert np.array_equal(h_u.numpy(), u) and np.array_equal(h_v.numpy(), v), "host and device paths disagree"
+    assert np.array_equal(h_u.numpy(), u_dev) and np.array_equal(h_v.numpy(), v_dev), "host and device paths disagree"
+    return {"value": world * npairs * W * H / (e2e_ms / args.steps * 1e-3) / 1e6, "unit": UNIT,
+            "h2d_bytes_per_step": int((npairs + 1) * W * H), "d2h_bytes_per_step": int(npairs * 2 * W * H * 4)}
 
-    # roofline of the dominant kernel (by total device time in the timed region)
+
+def choose_schedule(torch, prm, pattern, net, stream):
+    """The fastest seeded (iterations, jfMax) whose mean EPE on a separate
+    calibration sequence (another seed of the same generator) is at most the plain
+    engine's there.  Returns (schedule or None, table)."""
+    import numpy as np
+
+    from briefmatch_gb300 import synth
+
+    frames, flows = synth.make_sequence(SEED + 7777, W, H, FRAMES, vmax=VMAX)
+    d = torch.from_numpy(np.stack(frames)).cuda()
+    fp = [d[k].data_ptr() for k in range(FRAMES)]
+    u = torch.empty(PAIRS, H, W, device="cuda")
+    v = torch.empty(PAIRS, H, W, device="cuda")
+    up = [u[k].data_ptr() for k in range(PAIRS)]
+    vp = [v[k].data_ptr() for k in range(PAIRS)]
+
+    def run(eng):
+        sequence_step(eng, fp, up, vp, True)   # warm
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(3):
+            sequence_step(eng, fp, up, vp, True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / 3
+        epe = float(np.mean(mean_epe(u.cpu().numpy(), v.cpu().numpy(), flows)))
+        eng.clean()
+        return ms, epe
+
+    plain_ms, plain_epe = run(open_engine(torch, prm, pattern, stream))
+    table = [{"schedule": "plain %d/%d" % (prm.iterations, prm.jfMax), "ms": plain_ms, "epe": plain_epe}]
+    best = None
+    for sch in SCHEDULE_CANDIDATES:
+        ms, epe = run(open_engine(torch, prm, pattern, stream, net, sch))
+        table.append({"schedule": "seeded %d/%d" % sch, "ms": ms, "epe": epe})
+        if epe <= plain_epe and (best is None or ms < best[1]):
+            best = (sch, ms)
+    return (best[0] if best else None), table
+
+
+def run_engine(args, torch, world, rank):
+    import numpy as np
+
+    import briefmatch_gb300 as bm
+    from briefmatch_gb300 import learn
+
+    frames, flows = make_workload(rank)
+    batch_inputs = None if args.no_batched else make_batch_workload(args.batch_pairs)
+    prm = bm.BMParams.derive(W, H, UP, UP, N=NBITS)
+    pattern = prm.make_pattern(SEED)
+    # one explicit (non-default) stream carries the engine's work, the L2 flush and
+    # the timing events
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    d_frames = torch.from_numpy(np.stack(frames)).cuda()
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")  # > 129 MB L2
+
+    # plain engine (the reference's method and schedule)
+    plain = open_engine(torch, prm, pattern, stream)
+    rp = measure(args, torch, world, plain, d_frames, flows, stream, flush)
+
+    # learned-seeded engine: schedule chosen on a calibration sequence, then measured
+    learned = None
+    head, head_eng, head_name = rp, plain, "plain"
+    net = None
+    if not args.no_learned and os.path.exists(learn.DEFAULT_WEIGHTS):
+        net = learn.load_net(learn.DEFAULT_WEIGHTS, 1, H // 4, W // 4)
+        sch, table = choose_schedule(torch, prm, pattern, net, stream)
+        learned = {"weights": os.path.relpath(learn.DEFAULT_WEIGHTS, ROOT), "confidence": PROPOSAL_CONF,
+                   "calibration": table, "schedule": None}
+        if sch is not None:
+            seng = open_engine(torch, prm, pattern, stream, net, sch)
+            rl = measure(args, torch, world, seng, d_frames, flows, stream, flush)
+            learned.update({"schedule": {"iterations": sch[0], "jfMax": sch[1]}, "value": rl["value"],
+                            "ms_per_step": rl["ms_per_step"], "epe_mean": float(np.mean(rl["epe"])),
+                            "speedup_vs_plain": rp["ms_per_step"] / rl["ms_per_step"],
+                            "gpu_launches": int(rl["launches"])})
+            if np.mean(rl["epe"]) <= np.mean(rp["epe"]):
+                head, head_eng, head_name = rl, seng, "learned-seeded"
+            else:
+                seng.clean()
+
+    e2e = measure_e2e(args, torch, world, head_eng, frames, head["u"], head["v"], flush)
+
+    # roofline of the headline engine's dominant kernel (by total device time in the timed region)
+    kstats = head["kstats"]
     dom = max(kstats.items(), key=lambda kv: kv[1][1])[0]
     n_launch, dom_ms = kstats[dom]
     per_launch_ms = dom_ms / n_launch
@@ -312,19 +408,25 @@ def run_engine(args, torch, world, rank):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(prm, pattern, frames, args.cpu_pairs)
 
+    sched = learned["schedule"] if head_name != "plain" else {"iterations": prm.iterations, "jfMax": prm.jfMax}
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "u32 descriptors / int16 field / f32 flow", "data": "synthetic (seeded generator; see bench.py)",
-        "config": {"workload": WORKLOAD, "width": W, "height": H, "frames_per_step": FRAMES, "pairs_per_step": PAIRS,
-                   "upsampling": UP, "feature_length": NBITS, "grid": [prm.sx, prm.sy], "iterations": prm.iterations,
-                   "jfMax": prm.jfMax, "fsize": prm.fsize, "l2": "flushed (256 MB write) before every timed step",
+        "metric": METRIC, "value": head["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32 descriptors / int16 field / f32 flow",
+        "data": "synthetic (seeded generator; see bench.py)",
+        "config": {"workload": WORKLOAD % head_name, "engine": head_name, "width": W, "height": H,
+                   "frames_per_step": FRAMES, "pairs_per_step": PAIRS, "upsampling": UP, "feature_length": NBITS,
+                   "grid": [prm.sx, prm.sy], "iterations": sched["iterations"], "jfMax": sched["jfMax"],
+                   "fsize": prm.fsize, "l2": "flushed (256 MB write) before every timed step",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
-        "epe": {"mean": float(np.mean(epes)), "per_pair": [round(e, 4) for e in epes]},
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(FRAMES * W * H),
-                "d2h_bytes_per_step": int(PAIRS * 2 * W * H * 4)},
-        "gpu_launches": int(launches),
-        "clocks": clk.summary(),
+        "epe": {"mean": float(np.mean(head["epe"])), "per_pair": [round(e, 4) for e in head["epe"]],
+                "plain_mean": float(np.mean(rp["epe"]))},
+        "plain": {"value": rp["value"], "ms_per_step": rp["ms_per_step"], "epe_mean": float(np.mean(rp["epe"])),
+                  "gpu_launches": int(rp["launches"]), "iterations": prm.iterations, "jfMax": prm.jfMax},
+        "learned": learned,
+        "e2e": e2e,
+        "gpu_launches": int(head["launches"]),
+        "clocks": head["clocks"],
         "roofline": roofline,
         "kernels": kernels,
         "cpu_baseline": cpu,
@@ -332,7 +434,11 @@ def run_engine(args, torch, world, rank):
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
-    eng.clean()
+    plain.clean()
+    if head_eng is not plain:
+        head_eng.clean()
+    if net is not None:
+        net.close()
 
 
 BATCH_SEED = 20261204
@@ -492,7 +598,7 @@ def run_reference(args, torch, world, rank):
         "ms_per_step": tot / args.steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "impl": "reference", "dtype": "u32 descriptors / int16 field / f32 flow",
         "data": "synthetic (seeded generator; see bench.py)",
-        "config": {"workload": WORKLOAD, "width": W, "height": H, "upsampling": UP, "feature_length": NBITS,
+        "config": {"workload": WORKLOAD % "reference", "width": W, "height": H, "upsampling": UP, "feature_length": NBITS,
                    "step": "one pair of the sequence per step (bounded CPU sample)"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": nt, "kind": "port",
                          "sample": "one pair per step of the 1024x436 sequence, %d threads" % nt},

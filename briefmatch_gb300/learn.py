@@ -25,13 +25,21 @@ TRAIN_W, TRAIN_H, TRAIN_U, TRAIN_N = 512, 384, 2.9, 128
 TRAIN_SEED = 7_000_000
 
 
-def _pair(k):
-    """Pair k of the training set: the two 8-bit frames and the quarter-resolution
-    ground truth (quarter-resolution pixels), for held-out scoring."""
+SEQ_FRAMES = 8
+
+
+def _group(g, sequences):
+    """Training group g: with `sequences`, the 7 consecutive pairs of 8-frame
+    sequence g (flow redrawn per pair, each frame warped from the previous one, as
+    in the sequence workload); else the single pair g.  Each pair is (frame0,
+    frame1, quarter-resolution truth u, v in quarter-resolution pixels)."""
     from briefmatch_gb300 import synth
 
-    f0, f1, u, v = synth.make_pair(TRAIN_SEED + k, TRAIN_W, TRAIN_H, vmax=15.0)
-    return f0, f1, quarter(u) / 4.0, quarter(v) / 4.0
+    if sequences:
+        frames, flows = synth.make_sequence(TRAIN_SEED + g, TRAIN_W, TRAIN_H, SEQ_FRAMES, vmax=15.0)
+        return [(frames[k], frames[k + 1], quarter(u) / 4.0, quarter(v) / 4.0) for k, (u, v) in enumerate(flows)]
+    f0, f1, u, v = synth.make_pair(TRAIN_SEED + g, TRAIN_W, TRAIN_H, vmax=15.0)
+    return [(f0, f1, quarter(u) / 4.0, quarter(v) / 4.0)]
 
 
 def quarter(a):
@@ -40,46 +48,84 @@ def quarter(a):
     return a[:h4 * 4, :w4 * 4].reshape(h4, 4, w4, 4).mean(axis=(1, 3)).astype(np.float32)
 
 
-def engine_targets(pairs, iterations=4):
-    """BriefMatch's own flow for each (frame0, frame1) pair, computed by the batch API
-    with `iterations` propagation + random-search rounds: [n][h4][w4][3] float32
-    (u, v in quarter-resolution pixels, validity 1)."""
+def _batch_flows(pairs, iterations):
     import briefmatch_gb300 as bm
 
     prm = bm.BMParams.derive(TRAIN_W, TRAIN_H, TRAIN_U, TRAIN_U, N=TRAIN_N, iterations=iterations)
     b = bm.Batch([prm] * len(pairs))
     b.set_schedule(per_pair=1, use_graph=0)
-    b.load_frames(b.pack_frames([(p[0], p[1]) for p in pairs]))
+    b.load_frames(b.pack_frames(pairs))
     b.run()
     b.synchronize()
-    out = np.ones((len(pairs), TRAIN_H // 4, TRAIN_W // 4, 3), np.float32)
-    for k, (u, v) in enumerate(b.read_flows()):
-        out[k, ..., 0] = quarter(u) / 4.0
-        out[k, ..., 1] = quarter(v) / 4.0
+    out = [(u.copy(), v.copy()) for u, v in b.read_flows()]
     b.close()
     return out
 
 
-def build_set(torch, n, target_iterations, chunk=256, workers=None):
+def consistent(u, v, ub, vb, thr):
+    """Forward-backward check: pixel p keeps its forward vector when the backward
+    flow at p + F(p) (nearest pixel) brings it back within `thr` pixels."""
+    h, w = u.shape
+    ys, xs = np.mgrid[0:h, 0:w]
+    qx = np.rint(xs + u).astype(np.int64)
+    qy = np.rint(ys + v).astype(np.int64)
+    inside = (qx >= 0) & (qx < w) & (qy >= 0) & (qy < h)
+    qx, qy = np.clip(qx, 0, w - 1), np.clip(qy, 0, h - 1)
+    return inside & (np.hypot(u + ub[qy, qx], v + vb[qy, qx]) < thr)
+
+
+def engine_targets(pairs, iterations=4, consistency=1.0):
+    """BriefMatch's own flow for each (frame0, frame1) pair, computed by the batch API
+    with `iterations` propagation + random-search rounds, as [n][h4][w4][3] float32:
+    u, v in quarter-resolution pixels and a validity weight.  With `consistency`
+    > 0, BriefMatch also computes the backward flow of every pair; a pixel counts
+    only when the two agree within `consistency` pixels, each cell's target is the
+    mean over its consistent pixels and its weight their fraction."""
+    fw = _batch_flows([(p[0], p[1]) for p in pairs], iterations)
+    bw = _batch_flows([(p[1], p[0]) for p in pairs], iterations) if consistency > 0 else None
+    out = np.ones((len(pairs), TRAIN_H // 4, TRAIN_W // 4, 3), np.float32)
+    for k, (u, v) in enumerate(fw):
+        if bw is None:
+            out[k, ..., 0] = quarter(u) / 4.0
+            out[k, ..., 1] = quarter(v) / 4.0
+            continue
+        m = consistent(u, v, bw[k][0], bw[k][1], consistency).astype(np.float32)
+        cnt = quarter(m)
+        safe = np.maximum(cnt, 1e-6)
+        out[k, ..., 0] = np.where(cnt > 0, quarter(u * m) / safe, quarter(u)) / 4.0
+        out[k, ..., 1] = np.where(cnt > 0, quarter(v * m) / safe, quarter(v)) / 4.0
+        out[k, ..., 2] = cnt
+    return out
+
+
+def build_set(torch, n, target_iterations, chunk=256, workers=None, sequences=True, consistency=1.0):
     """Generate n training pairs chunk by chunk (spawn-started CPU pool, so the pool
     never inherits a CUDA context) and keep frames and engine targets on the device.
     Returns (frames0 [n][H][W] u8, frames1, targets [n][h4][w4][3], gt [n][h4][w4][2])."""
     import multiprocessing as mp
+
+    from functools import partial
 
     workers = workers or min(16, os.cpu_count() or 1)
     f0 = torch.empty(n, TRAIN_H, TRAIN_W, dtype=torch.uint8, device="cuda")
     f1 = torch.empty_like(f0)
     tgt = torch.empty(n, TRAIN_H // 4, TRAIN_W // 4, 3, device="cuda")
     gt = np.empty((n, TRAIN_H // 4, TRAIN_W // 4, 2), np.float32)
+    per = SEQ_FRAMES - 1 if sequences else 1
+    groups = (n + per - 1) // per
+    gchunk = max(1, chunk // per)
+    s = 0
     with mp.get_context("spawn").Pool(workers) as pool:
-        for s in range(0, n, chunk):
-            part = pool.map(_pair, range(s, min(n, s + chunk)), chunksize=8)
+        for g0 in range(0, groups, gchunk):
+            part = [p for grp in pool.map(partial(_group, sequences=sequences), range(g0, min(groups, g0 + gchunk)))
+                    for p in grp][:n - s]
             k = len(part)
             f0[s:s + k] = torch.from_numpy(np.stack([p[0] for p in part]))
             f1[s:s + k] = torch.from_numpy(np.stack([p[1] for p in part]))
-            tgt[s:s + k] = torch.from_numpy(engine_targets(part, target_iterations))
+            tgt[s:s + k] = torch.from_numpy(engine_targets(part, target_iterations, consistency))
             gt[s:s + k, ..., 0] = np.stack([p[2] for p in part])
             gt[s:s + k, ..., 1] = np.stack([p[3] for p in part])
+            s += k
     return f0, f1, tgt, gt
 
 
@@ -136,7 +182,8 @@ def train(args):
     from briefmatch_gb300.proposal import ProposalNet
 
     t0 = time.time()
-    f0, f1, tgt, gt = build_set(torch, args.pairs, args.target_iterations)
+    f0, f1, tgt, gt = build_set(torch, args.pairs, args.target_iterations, sequences=not args.single_pairs,
+                                consistency=args.consistency)
     torch.cuda.synchronize()
     t_data = time.time() - t0
     n = args.pairs
@@ -151,7 +198,8 @@ def train(args):
     os.makedirs(os.path.dirname(os.path.abspath(args.out)), exist_ok=True)
     net.save(args.out)
     report = {"pairs": n, "heldout": nval, "size": [TRAIN_W, TRAIN_H], "epochs": args.epochs, "batch": args.batch,
-              "lr": args.lr, "target_iterations": args.target_iterations,
+              "lr": args.lr, "target_iterations": args.target_iterations, "consistency_px": args.consistency,
+              "data": "single pairs" if args.single_pairs else "consecutive pairs of 8-frame sequences",
               "seconds": {"data_and_targets": t_data, "train": t_train},
               "heldout_epe_vs_briefmatch_px": e_tgt, "heldout_epe_vs_truth_px": e_gt,
               "heldout_confident_fraction": conf, "loss_history": hist}
@@ -239,18 +287,24 @@ def main(argv=None):
     t.add_argument("--lr", type=float, default=2e-3)
     t.add_argument("--seed", type=int, default=1)
     t.add_argument("--target-iterations", type=int, default=4)
+    t.add_argument("--consistency", type=float, default=1.0,
+                   help="forward-backward agreement (px) a target pixel needs; 0 keeps every pixel")
+    t.add_argument("--single-pairs", action="store_true", help="independent pairs instead of sequences")
     t.add_argument("--out", default=DEFAULT_WEIGHTS)
     e = sub.add_parser("eval")
     e.add_argument("--weights", default=DEFAULT_WEIGHTS)
     e.add_argument("--width", type=int, default=1024)
     e.add_argument("--height", type=int, default=436)
     e.add_argument("--frames", type=int, default=8)
+    e.add_argument("--seed", type=int, default=20261203)
+    e.add_argument("--schedules", default="1/4,1/16,1/64,2/256", help="iterations/jfMax list")
     args = ap.parse_args(argv)
     if args.cmd == "train":
         train(args)
     else:
         net = load_net(args.weights, 1, args.height // 4, args.width // 4)
-        for row in evaluate(net, args.width, args.height, args.frames):
+        sch = [tuple(int(x) for x in t.split("/")) for t in args.schedules.split(",")]
+        for row in evaluate(net, args.width, args.height, args.frames, seed=args.seed, schedules=sch):
             print(json.dumps(row))
 
 

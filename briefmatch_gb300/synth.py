@@ -4,8 +4,10 @@ These stand in for the Middlebury-style pairs the reference is demonstrated on
 (the public benchmark data is not used).  Generator, per the workload
 description:
   frame 1  mid-grey 128 + 40 Gaussian blobs (sigma U[5,40] px, amplitude
-           U[-80,80]) + band-limited noise (i.i.d. N(0,10) blurred with a
-           3 px Gaussian)
+           U[-80,80]) + band-limited noise of standard deviation 10 (i.i.d.
+           normal noise blurred with a 3 px Gaussian, then rescaled to sigma 10:
+           blurring alone would leave sigma ~0.94, below frame 2's sensor noise,
+           and the pairs would carry no texture to match)
   flow     global affine (|t| <= 4 px, rotation <= 2 deg, scale 0.97-1.03)
            plus 3-6 rectangles moving rigidly (|v| <= vmax px)
   frame 2  frame 1 warped by the flow (bilinear, backward), + i.i.d. N(0, 2)
@@ -51,8 +53,8 @@ def make_frame(rng, w, h, blobs=40):
             continue
         sub = ((xx[y0:y1, x0:x1] - cx) ** 2 + (yy[y0:y1, x0:x1] - cy) ** 2) / (2 * s * s)
         img[y0:y1, x0:x1] += a * np.exp(-sub)
-    noise = rng.normal(0, 10, size=(h, w))
-    img += _gauss_blur(noise, 3.0)
+    noise = _gauss_blur(rng.normal(0, 10, size=(h, w)), 3.0)
+    img += noise * (10.0 / max(float(noise.std()), 1e-9))
     return img
 
 

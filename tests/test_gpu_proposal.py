@@ -178,15 +178,15 @@ WEIGHTS = learn.DEFAULT_WEIGHTS
 @pytest.mark.skipif(not os.path.exists(WEIGHTS), reason="trained proposal weights not present")
 def test_committed_weights_gain():
     """EPE vs the truth at equal schedules, with and without the trained proposal, on
-    a held-out synthetic sequence at the training size: seeding never loses, wins
-    clearly at the short schedules, and the short seeded schedule is at least as
-    good as the plain default (2 iterations, jfMax 256)."""
+    a held-out synthetic sequence at the training size: seeding never loses, more
+    than halves the error at the shortest schedule, and one seeded iteration with
+    jump maximum 64 is at least as good as the plain default (2 iterations, 256)."""
     W, H = learn.TRAIN_W, learn.TRAIN_H
     net = learn.load_net(WEIGHTS, 1, H // 4, W // 4)
-    rows = learn.evaluate(net, W, H, frames=5, seed=424242, schedules=((1, 4), (1, 16), (2, 256)), reps=1,
+    rows = learn.evaluate(net, W, H, frames=5, seed=424242, schedules=((1, 4), (1, 64), (2, 256)), reps=1,
                           torch=torch)
     by = {(r["iterations"], r["jfMax"]): r for r in rows}
     for r in rows:
         assert r["seeded_epe"] <= r["plain_epe"] * 1.02, r
-    assert by[(1, 4)]["seeded_epe"] < 0.9 * by[(1, 4)]["plain_epe"], by[(1, 4)]
-    assert by[(1, 16)]["seeded_epe"] <= by[(2, 256)]["plain_epe"] * 1.02, rows
+    assert by[(1, 4)]["seeded_epe"] < 0.5 * by[(1, 4)]["plain_epe"], by[(1, 4)]
+    assert by[(1, 64)]["seeded_epe"] <= by[(2, 256)]["plain_epe"], rows
