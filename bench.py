@@ -64,6 +64,8 @@ def parse():
     ap.add_argument("--no-batched", action="store_true", help="skip the 64-pair batched workload")
     ap.add_argument("--batch-pairs", type=int, default=64)
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-seeded engine")
+    ap.add_argument("--schedule", default=None,
+                    help="ITERATIONS/JFMAX for the learned-seeded engine instead of choosing it by calibration")
     return ap.parse_args()
 
 
@@ -230,8 +232,10 @@ def mean_epe(u, v, flows):
 def measure(args, torch, world, eng, d_frames, flows, stream, flush):
     """Device throughput of one engine over the sequence: W warm-up steps, then K
     steps timed with CUDA events on the engine stream, L2 flushed before each step
-    (outside the events), per-kernel CUDA-event profile and SM clocks sampled over
-    the timed region."""
+    (outside the events), SM clocks sampled over the timed region.  A second run of
+    K steps records a CUDA event pair around every launch (the engine's per-kernel
+    profile, which the roofline uses); its own step time is reported beside the
+    first, which carries no per-launch events."""
     npairs = d_frames.shape[0] - 1
     d_u = torch.empty(npairs, H, W, device="cuda")
     d_v = torch.empty(npairs, H, W, device="cuda")
@@ -241,29 +245,38 @@ def measure(args, torch, world, eng, d_frames, flows, stream, flush):
     for _ in range(args.warmup):
         sequence_step(eng, fp, up, vp, True)
     torch.cuda.synchronize()
-    eng.profile(True)
-    eng.profile_reset()
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    launches0 = eng.launch_count()
-    with ClockSampler(torch.cuda.current_device()) as clk:
-        barrier(torch, world)
-        torch.cuda.synchronize()
-        for i in range(args.steps):
-            flush.zero_()
-            starts[i].record(stream)
-            sequence_step(eng, fp, up, vp, True)
-            ends[i].record(stream)
-        torch.cuda.synchronize()
-        barrier(torch, world)
-    launches = eng.launch_count() - launches0
-    total_ms = max_over_ranks(torch, world, sum(s.elapsed_time(e) for s, e in zip(starts, ends)))
-    kstats = eng.profile_read()
-    eng.profile(False)
-    ms = total_ms / args.steps
+
+    def timed(profiled):
+        if profiled:
+            eng.profile(True)
+            eng.profile_reset()
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        launches0 = eng.launch_count()
+        with ClockSampler(torch.cuda.current_device()) as clk:
+            barrier(torch, world)
+            torch.cuda.synchronize()
+            for i in range(args.steps):
+                flush.zero_()
+                starts[i].record(stream)
+                sequence_step(eng, fp, up, vp, True)
+                ends[i].record(stream)
+            torch.cuda.synchronize()
+            barrier(torch, world)
+        launches = eng.launch_count() - launches0
+        total_ms = max_over_ranks(torch, world, sum(s.elapsed_time(e) for s, e in zip(starts, ends)))
+        kstats = None
+        if profiled:
+            kstats = eng.profile_read()
+            eng.profile(False)
+        return total_ms / args.steps, launches, clk.summary(), kstats
+
+    ms, launches, clocks, _ = timed(False)
+    ms_prof, _, _, kstats = timed(True)
     u, v = d_u.cpu().numpy(), d_v.cpu().numpy()
     return {"ms_per_step": ms, "value": world * npairs * W * H / (ms * 1e-3) / 1e6, "launches": launches,
-            "kstats": kstats, "clocks": clk.summary(), "epe": mean_epe(u, v, flows), "u": u, "v": v}
+            "kstats": kstats, "ms_per_step_profiled": ms_prof, "clocks": clocks, "epe": mean_epe(u, v, flows),
+            "u": u, "v": v}
 
 
 def measure_e2e(args, torch, world, eng, frames, u_dev, v_dev, flush):
@@ -337,6 +350,34 @@ def choose_schedule(torch, prm, pattern, net, stream):
     return (best[0] if best else None), table
 
 
+def net_forward_timing(torch, net, d_frames, stream, reps=50):
+    """Device time of the proposal network's input preparation + forward pass for one
+    1024x436 pair (quarter resolution 256x109), and its tensor-core rate."""
+    from briefmatch_gb300.proposal import flops_per_pixel
+
+    h4, w4 = H // 4, W // 4
+    out = torch.empty(1, h4, w4, 3, device="cuda")
+    st = stream.cuda_stream
+
+    def once():
+        net.prepare(0, d_frames[0].data_ptr(), d_frames[1].data_ptr(), W, H, st)
+        net.forward(1, h4, w4, out.data_ptr(), st)
+
+    for _ in range(5):
+        once()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        once()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    flops = flops_per_pixel() * h4 * w4
+    return {"ms_per_pair": ms, "gflop_per_pair": flops / 1e9, "tflop_s": flops / (ms * 1e-3) / 1e12,
+            "note": "input preparation + 6 conv layers, 1 pair, back to back"}
+
+
 def run_engine(args, torch, world, rank):
     import numpy as np
 
@@ -364,9 +405,12 @@ def run_engine(args, torch, world, rank):
     net = None
     if not args.no_learned and os.path.exists(learn.DEFAULT_WEIGHTS):
         net = learn.load_net(learn.DEFAULT_WEIGHTS, 1, H // 4, W // 4)
-        sch, table = choose_schedule(torch, prm, pattern, net, stream)
+        if args.schedule:
+            sch, table = tuple(int(x) for x in args.schedule.split("/")), "given on the command line"
+        else:
+            sch, table = choose_schedule(torch, prm, pattern, net, stream)
         learned = {"weights": os.path.relpath(learn.DEFAULT_WEIGHTS, ROOT), "confidence": PROPOSAL_CONF,
-                   "calibration": table, "schedule": None}
+                   "calibration": table, "schedule": None, "net_forward": net_forward_timing(torch, net, d_frames, stream)}
         if sch is not None:
             seng = open_engine(torch, prm, pattern, stream, net, sch)
             rl = measure(args, torch, world, seng, d_frames, flows, stream, flush)
@@ -396,13 +440,17 @@ def run_engine(args, torch, world, rank):
         "algorithmic_bytes_per_launch": abytes, "launch_ms": per_launch_ms, "launches": n_launch,
         "share_of_kernel_time": dom_ms / total_k if total_k else None,
         "traffic": ncu_traffic(dom),
+        "timed_region": "second run of the K timed steps with a CUDA event pair around every launch "
+                        "(%.3f ms per step there vs %.3f without)" % (head["ms_per_step_profiled"], head["ms_per_step"]),
     }
     kernels = {k: {"launches": c, "ms": round(t, 4), "share": round(t / total_k, 4)} for k, (c, t) in
                sorted(kstats.items(), key=lambda kv: -kv[1][1])}
 
     batched = None
     if batch_inputs is not None:
-        batched = run_batched(args, torch, *batch_inputs)
+        bsched = learned["schedule"] if learned and learned.get("schedule") else None
+        batched = run_batched(args, torch, *batch_inputs, net=net if bsched else None,
+                              schedule=(bsched["iterations"], bsched["jfMax"]) if bsched else None)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -466,10 +514,12 @@ def make_batch_workload(pairs):
     return sizes, data
 
 
-def run_batched(args, torch, sizes, data):
+def run_batched(args, torch, sizes, data, net=None, schedule=None):
     """The batched workload: all pairs through one autotuned batch step (persistent
     matching launch and/or per-level launches, replayed as a CUDA graph) against the
-    same pairs run one after another through per-pair contexts (plain launches)."""
+    same pairs run one after another through per-pair contexts (plain launches); with
+    a proposal network, the same batch again with every pair seeded by it at the
+    given (iterations, jfMax)."""
     import numpy as np
 
     import briefmatch_gb300 as bm
@@ -497,6 +547,31 @@ def run_batched(args, torch, sizes, data):
     flows = b.read_flows()
     epe = float(np.mean([np.mean(np.hypot(f[0] - d[2], f[1] - d[3])) for f, d in zip(flows, data)]))
     sched = b.schedule()
+    learned = None
+    if net is not None:
+        from briefmatch_gb300.proposal import ProposalNet
+
+        bnet = ProposalNet(1, max(h for _, h in sizes) // 4, max(w for w, _ in sizes) // 4)
+        bnet.set_params(net.params())
+        b.set_proposal(bnet, PROPOSAL_CONF, schedule[0], schedule[1])
+        lrep = b.autotune(None, reps=2)
+        for _ in range(args.warmup):
+            b.run()
+        b.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        for s0, s1 in ev:
+            s0.record(stream)
+            b.run()
+            s1.record(stream)
+        b.synchronize()
+        lms = sum(s0.elapsed_time(s1) for s0, s1 in ev) / args.steps
+        lflows = b.read_flows()
+        lepe = float(np.mean([np.mean(np.hypot(f[0] - d[2], f[1] - d[3])) for f, d in zip(lflows, data)]))
+        learned = {"schedule": {"iterations": schedule[0], "jfMax": schedule[1]}, "value": out_px / (lms * 1e-3) / 1e6,
+                   "ms_per_step": lms, "epe_mean": lepe, "speedup_vs_plain_batch": batch_ms / lms,
+                   "autotune": lrep, "batch_schedule": b.schedule()}
+        b.set_proposal(None)
+        bnet.close()
     b.close()
     del d_packed
 
@@ -537,6 +612,7 @@ def run_batched(args, torch, sizes, data):
         "sequential_value": out_px / (seq_ms * 1e-3) / 1e6, "sequential_ms_per_step": seq_ms,
         "speedup_vs_sequential": seq_ms / batch_ms,
         "schedule": sched, "autotune": report, "epe_mean": epe,
+        "learned": dict(learned, speedup_vs_plain_sequential=seq_ms / learned["ms_per_step"]) if learned else None,
     }
 
 

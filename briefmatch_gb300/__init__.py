@@ -104,6 +104,7 @@ def _declare(lib):
         "bm_profile_reset": (c.c_int, [c.c_void_p]),
         "bm_profile_read": (c.c_int, [c.c_void_p, c.c_void_p, c.c_uint32, P(c.c_uint32)]),
         "bm_set_proposal": (c.c_int, [c.c_void_p, c.c_void_p, c.c_float, c.c_uint32, c.c_uint32]),
+        "bm_batch_set_proposal": (c.c_int, [c.c_void_p, c.c_void_p, c.c_float, c.c_uint32, c.c_uint32]),
         "bm_seed": (c.c_int, [c.c_void_p, c.c_int, c.c_void_p, c.c_uint32, c.c_uint32, c.c_float]),
         "bm_refine_noalloc": (c.c_int, [c.c_void_p, c.c_void_p, c.c_void_p, c.c_void_p, c.c_void_p, c.c_uint32,
                                         c.c_uint32, c.c_uint32, c.c_float, c.c_float, c.c_float, c.c_void_p]),
@@ -490,6 +491,11 @@ class Batch:
 
     def launch_count(self):
         return int(lib().bm_batch_launch_count(self._b))
+
+    def set_proposal(self, net, conf_threshold=0.5, iterations=1, jf_max=16):
+        """Seed every pair with a ProposalNet (None detaches); see bm_batch_set_proposal."""
+        check(lib().bm_batch_set_proposal(self._b, net.handle if net is not None else None, conf_threshold,
+                                          iterations, jf_max))
 
 
 def set_proposal(engine, net, conf_threshold=0.5, iterations=1, jf_max=16):

@@ -37,7 +37,7 @@ struct PairDev {
     float dist, mx, my, cE, cI, cS;
     int first_up_tile_x;   // tiles per row on the up-sampled grid
     int first_in_tile_x;   // tiles per row at input resolution (32x8)
-    int first_tri_tile_x;  // tiles per row for the trilateral filter (32x16)
+    int first_tri_tile_x;  // tiles per row for the trilateral filter (TX x TRI_BY)
     const uint8_t* frame[2];
     float* guide;          // frame 0 as float (the trilateral guide)
     float* up;
@@ -64,7 +64,7 @@ struct BatchDev {
     const PairDev* pairs;
     const unsigned int* pre_up;   // [count+1] exclusive prefix of up-sampled-grid tiles
     const unsigned int* pre_in;   // input-resolution 32x8 tiles
-    const unsigned int* pre_tri;  // trilateral 32x16 tiles
+    const unsigned int* pre_tri;  // trilateral TX x TRI_BY tiles
     int lo, hi;
     int N;
 };
@@ -307,6 +307,11 @@ struct bm_batch {
     cudaGraph_t graph = nullptr;
     bool graph_valid = false;
     uint64_t launches = 0;
+    // learned proposal (bm_batch_set_proposal): per-pair schedule only
+    bm_net* net = nullptr;
+    float net_logit_min = 0.0f;
+    uint32_t net_iterations = 0, net_jfMax = 0;
+    float* d_pred = nullptr;   // [h4][w4][3] of the pair being seeded (pairs run in stream order)
 };
 
 namespace {
@@ -409,15 +414,30 @@ bm_status enqueue_pair(bm_batch* b, const bm_batch_schedule& s, int j)
         rev ^= s.snake ? 1 : 0;
     }
     int cur = 0;
-    BB_CUDA(initialize(d.F[0], d.F[1], d.flow[cur], d.flow[cur ^ 1], d.cost, d.sx, d.sy, (int)b->nsp, 1, rev, st));
+    uint32_t iterations = b->iterations, jfMax = b->jfMax;
+    if (b->net) {
+        // the proposal for this pair, then the seeded initialisation (bm_seed's rule)
+        const uint32_t w4 = (uint32_t)d.sx_in / 4, h4 = (uint32_t)d.sy_in / 4;
+        bm_status nst = bm_net_prepare(b->net, 0, d.frame[0], d.frame[1], (uint32_t)d.sx_in, (uint32_t)d.sy_in, st);
+        if (nst == BM_OK) nst = bm_net_forward(b->net, 1, h4, w4, b->d_pred, st);
+        if (nst != BM_OK) return nst;
+        const float scx = 4.0f * (float)d.sx / (float)d.sx_in, scy = 4.0f * (float)d.sy / (float)d.sy_in;
+        BB_CUDA(seed_field(d.F[0], d.F[1], d.flow[cur], d.flow[cur ^ 1], d.cost, d.sx, d.sy, (int)b->nsp, 1, b->d_pred,
+                           (int)w4, (int)h4, scx, scy, b->net_logit_min, st));
+        iterations = b->net_iterations;
+        if (b->net_jfMax) jfMax = b->net_jfMax;
+        b->launches += 8;
+    } else {
+        BB_CUDA(initialize(d.F[0], d.F[1], d.flow[cur], d.flow[cur ^ 1], d.cost, d.sx, d.sy, (int)b->nsp, 1, rev, st));
+    }
     rev ^= s.snake ? 1 : 0;
     cur ^= 1;
     int pd = -1;
     int levels = 0;
-    for (int q = (int)b->jfMax; q > 0; q /= 2) levels++;
-    for (uint32_t it = 0; it < b->iterations; it++) {
+    for (int q = (int)jfMax; q > 0; q /= 2) levels++;
+    for (uint32_t it = 0; it < iterations; it++) {
         int lvl = 0;
-        for (int q = (int)b->jfMax; q > 0; q /= 2, lvl++) {
+        for (int q = (int)jfMax; q > 0; q /= 2, lvl++) {
             RsArgs rs;
             rs.enabled = lvl == levels - 1;
             rs.mode = b->rng;
@@ -437,7 +457,7 @@ bm_status enqueue_pair(bm_batch* b, const bm_batch_schedule& s, int j)
     } else {
         BB_CUDA(flow_to_planes(d.flow[cur], d.flow_in, d.flow_in + ni, ni, st));
     }
-    b->launches += 6 + (uint64_t)b->iterations * levels;
+    b->launches += 6 + (uint64_t)iterations * levels - (b->net ? 1 : 0);
     return BM_OK;
 }
 
@@ -614,6 +634,7 @@ std::string shape_key(const bm_batch* b)
     std::ostringstream ss;
     ss << prop.name << "|pairs=" << b->count << "|N=" << b->N << "|it=" << b->iterations << "|jf=" << b->jfMax
        << "|upMpx=" << (px + 500000) / 1000000;
+    if (b->net) ss << "|seeded=" << b->net_iterations << "/" << b->net_jfMax;
     return ss.str();
 }
 
@@ -866,6 +887,7 @@ bm_status bm_batch_destroy(bm_batch* b)
     if (b->d_pairs) cudaFree(b->d_pairs);
     if (b->d_pre) cudaFree(b->d_pre);
     if (b->d_sync) cudaFree(b->d_sync);
+    if (b->d_pred) cudaFree(b->d_pred);
     if (b->own_stream) cudaStreamDestroy(b->own_stream);
     delete b;
     return BM_OK;
@@ -956,6 +978,8 @@ bm_status bm_batch_flow_ptr(bm_batch* b, uint32_t pair, float** d_u, float** d_v
 bm_status bm_batch_set_schedule(bm_batch* b, const bm_batch_schedule* s)
 {
     if (!b || !s) return bfail(BM_ERR_INVALID, "bm_batch_set_schedule: null argument");
+    if (b->net && !s->per_pair)
+        return bfail(BM_ERR_INVALID, "bm_batch_set_schedule: a batch with a proposal runs the per-pair schedule");
     b->sched = *s;
     if (b->sched.blocks_per_sm == 0 || (int)b->sched.blocks_per_sm > b->coop_blocks_per_sm)
         b->sched.blocks_per_sm = (uint32_t)b->coop_blocks_per_sm;
@@ -994,6 +1018,30 @@ bm_status bm_batch_synchronize(bm_batch* b)
 }
 
 uint64_t bm_batch_launch_count(const bm_batch* b) { return b ? b->launches : 0; }
+
+bm_status bm_batch_set_proposal(bm_batch* b, bm_net* net, float conf_threshold, uint32_t iterations, uint32_t jfMax)
+{
+    if (!b) return bfail(BM_ERR_INVALID, "null batch");
+    if (net && !(conf_threshold > 0.0f && conf_threshold < 1.0f))
+        return bfail(BM_ERR_INVALID, "bm_batch_set_proposal: confidence threshold must lie in (0, 1)");
+    if (net) {
+        size_t cells = 0;
+        for (const auto& p : b->prm) {
+            if (p.sx_in < 4 || p.sy_in < 4) return bfail(BM_ERR_LIMIT, "bm_batch_set_proposal: frame too small");
+            cells = std::max(cells, (size_t)(p.sx_in / 4) * (p.sy_in / 4));
+        }
+        if (!b->d_pred && cudaMalloc((void**)&b->d_pred, cells * 3 * sizeof(float)) != cudaSuccess)
+            return bfail(BM_ERR_NOMEM, "bm_batch_set_proposal: prediction buffer allocation failed");
+        b->sched.per_pair = 1;
+        b->sched.persistent = 0;
+    }
+    b->net = net;
+    b->net_logit_min = net ? std::log(conf_threshold / (1.0f - conf_threshold)) : 0.0f;
+    b->net_iterations = iterations;
+    b->net_jfMax = jfMax;
+    destroy_graph(b);
+    return BM_OK;
+}
 
 // Times each candidate schedule on this batch (after one untimed run each) and keeps
 // the fastest; with cache_path, a previous choice for the same shape is reused and
@@ -1042,8 +1090,14 @@ bm_status bm_batch_autotune(bm_batch* b, const char* cache_path, int reps, char*
         s.wave_bytes = 0;
         cands.push_back(s);
     }
+    {
+        bm_batch_schedule s = cands.back();
+        s.use_graph = 0;   // per-pair launches without the graph
+        cands.push_back(s);
+    }
     const uint64_t waves[4] = {0ull, 64 * MB, 96 * MB, 160 * MB};
     for (uint64_t wave : waves) {
+        if (b->net) break;   // the proposal runs in the per-pair schedule only
         for (uint32_t persistent = 0; persistent <= 1; persistent++) {
             bm_batch_schedule s = b->sched;
             s.per_pair = 0;

@@ -504,18 +504,24 @@ __device__ __forceinline__ void median_px(const float* __restrict__ in, float* _
 // used four times and every arithmetic instruction serves two outputs.  The
 // (2s + TX) x (2s + TRI_BY) neighbourhood is staged in shared memory with
 // clamp-to-edge addressing.  The three Gaussians are one exp2 of the summed
-// exponents; the column factor exp2(-cS*i^2) is applied once per column (the inner
-// loop runs down a column); row factors outside the window are -inf (weight 0).
+// exponents: with kE = sqrt(cE) and kI = sqrt(cI), each scaled difference is one
+// FMA against the centre's negated scaled value (kE*u - kE*uc), the squared terms
+// accumulate by FMA onto the row term j^2*cS, and exp2 takes the negated sum --
+// six FP32 operations per tap and output before the three accumulations.  The
+// column factor exp2(-cS*i^2) is applied once per column (the inner loop runs down
+// a column); row terms outside the window are +inf (weight 0).
 // `smem` must hold tri_smem_bytes(s).
 // ---------------------------------------------------------------------------
 constexpr int TRI_R = 4;                // outputs per thread (two f32x2 pairs)
-constexpr int TRI_TY = 4;               // thread rows per block
-constexpr int TRI_BY = TRI_TY * TRI_R;  // output rows per block (32x16 outputs)
+constexpr int TRI_TY = 8;               // thread rows per block
+constexpr int TRI_BY = TRI_TY * TRI_R;  // output rows per block (32x32 outputs)
 
 __host__ __device__ inline size_t tri_smem_bytes(int s)
 {
     return (size_t)(2 * s + TRI_R - 1) * sizeof(float4) + (size_t)(TX + 2 * s) * (TRI_BY + 2 * s) * 3 * sizeof(float);
 }
+
+__device__ __forceinline__ f2x ex2n_2(f2x a) { return pk2(exp2f(-lo2(a)), exp2f(-hi2(a))); }
 
 __device__ __forceinline__ void trilateral_block(const float* __restrict__ U, const float* __restrict__ V,
                                                  const float* __restrict__ Um, const float* __restrict__ Vm,
@@ -525,7 +531,7 @@ __device__ __forceinline__ void trilateral_block(const float* __restrict__ U, co
 {
     const int TW = TX + 2 * s, TH = TRI_BY + 2 * s;
     const int NR = 2 * s + TRI_R - 1;        // source rows a thread walks per column
-    float4* rowf = smem4;                    // [NR] exponents of the row factor for outputs r=0..3
+    float4* rowf = smem4;                    // [NR] row terms j^2*cS for outputs r=0..3
     float2* suv = reinterpret_cast<float2*>(smem4 + NR);
     float* sI = reinterpret_cast<float*>(suv + TW * TH);
     const int x0 = bx0 - s, y0 = by0 - s;
@@ -542,7 +548,7 @@ __device__ __forceinline__ void trilateral_block(const float* __restrict__ U, co
 #pragma unroll
         for (int r = 0; r < TRI_R; r++) {
             const int j = m - r - s;  // vertical offset of this source row for output r
-            t[r] = (j >= -s && j < s) ? -(float)(j * j) * cS : -__int_as_float(0x7f800000);
+            t[r] = (j >= -s && j < s) ? (float)(j * j) * cS : __int_as_float(0x7f800000);
         }
         rowf[m] = make_float4(t[0], t[1], t[2], t[3]);
     }
@@ -551,19 +557,20 @@ __device__ __forceinline__ void trilateral_block(const float* __restrict__ U, co
     const int x = bx0 + threadIdx.x;
     const int yb = by0 + threadIdx.y * TRI_R;
     if (x >= sx || yb >= sy) return;
+    const float kE = sqrtf(cE), kI = sqrtf(cI);
     float umc[TRI_R], vmc[TRI_R], Ic[TRI_R];
 #pragma unroll
     for (int r = 0; r < TRI_R; r++) {
         const int yy = min(sy - 1, yb + r);
         const size_t o = (size_t)x + (size_t)yy * sx;
-        umc[r] = __ldg(Um + o);
-        vmc[r] = __ldg(Vm + o);
-        Ic[r] = sI[(threadIdx.y * TRI_R + r + s) * TW + threadIdx.x + s];
+        umc[r] = -kE * __ldg(Um + o);
+        vmc[r] = -kE * __ldg(Vm + o);
+        Ic[r] = -kI * sI[(threadIdx.y * TRI_R + r + s) * TW + threadIdx.x + s];
     }
     const f2x umA = pk2(umc[0], umc[1]), umB = pk2(umc[2], umc[3]);
     const f2x vmA = pk2(vmc[0], vmc[1]), vmB = pk2(vmc[2], vmc[3]);
     const f2x IA = pk2(Ic[0], Ic[1]), IB = pk2(Ic[2], Ic[3]);
-    const f2x nE = pk2(-cE, -cE), nI = pk2(-cI, -cI);
+    const f2x kEE = pk2(kE, kE), kII = pk2(kI, kI);
     f2x ufA = 0, ufB = 0, vfA = 0, vfB = 0, WA = 0, WB = 0;  // 0 bits = (0.0f, 0.0f)
     const int row0 = threadIdx.y * TRI_R;
     for (int i = -s; i < s; i++) {
@@ -576,19 +583,17 @@ __device__ __forceinline__ void trilateral_block(const float* __restrict__ U, co
             const float i1 = colI[m * TW];
             const float4 rf = rowf[m];
             const f2x uu = pk2(uv.x, uv.x), vv = pk2(uv.y, uv.y), ii = pk2(i1, i1);
-            f2x du = sub2(uu, umA), dv = sub2(vv, vmA), dI = sub2(ii, IA);
-            f2x e = fma2(dv, dv, mul2(du, du));
-            f2x arg = fma2(mul2(dI, dI), nI, fma2(e, nE, pk2(rf.x, rf.y)));
-            f2x w = ex2_2(arg);
+            f2x du = fma2(uu, kEE, umA), dv = fma2(vv, kEE, vmA), dI = fma2(ii, kII, IA);
+            f2x q = fma2(dI, dI, fma2(dv, dv, fma2(du, du, pk2(rf.x, rf.y))));
+            f2x w = ex2n_2(q);
             cuA = fma2(w, uu, cuA);
             cvA = fma2(w, vv, cvA);
             cwA = add2(cwA, w);
-            du = sub2(uu, umB);
-            dv = sub2(vv, vmB);
-            dI = sub2(ii, IB);
-            e = fma2(dv, dv, mul2(du, du));
-            arg = fma2(mul2(dI, dI), nI, fma2(e, nE, pk2(rf.z, rf.w)));
-            w = ex2_2(arg);
+            du = fma2(uu, kEE, umB);
+            dv = fma2(vv, kEE, vmB);
+            dI = fma2(ii, kII, IB);
+            q = fma2(dI, dI, fma2(dv, dv, fma2(du, du, pk2(rf.z, rf.w))));
+            w = ex2n_2(q);
             cuB = fma2(w, uu, cuB);
             cvB = fma2(w, vv, cvB);
             cwB = add2(cwB, w);

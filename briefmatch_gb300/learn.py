@@ -158,6 +158,17 @@ def train_net(torch, net, f0, f1, tgt, idx_train, epochs, batch, lr, seed=1, log
     return hist
 
 
+def batch_loss(torch, net, f0, f1, tgt, idx):
+    """(flow loss, confidence loss) of the network on pairs idx, without an update."""
+    h4, w4 = TRAIN_H // 4, TRAIN_W // 4
+    stream = torch.cuda.current_stream().cuda_stream
+    for j, i in enumerate(idx):
+        net.prepare(j, f0[i].data_ptr(), f1[i].data_ptr(), TRAIN_W, TRAIN_H, stream)
+    d = tgt[torch.as_tensor(list(idx), device="cuda")].contiguous()
+    loss = net.train_step(len(idx), h4, w4, d.data_ptr(), 0.0, 0, stream)
+    return float(loss[0]), float(loss[1])
+
+
 def score(torch, net, f0, f1, tgt, gt, idx):
     """Mean end-point error (input pixels) of the proposal against BriefMatch's flow
     and against the truth, and the fraction of confident cells, over pairs idx."""

@@ -40,6 +40,14 @@ def _declare():
     _declared = True
 
 
+def flops_per_pixel():
+    """Multiply-add FLOPs of one forward pass per quarter-resolution pixel (real
+    channels: 3x3 taps, 2 -> 32, four 32 -> 32, 32 -> 3)."""
+    cin = [2, 32, 32, 32, 32, 32]
+    cout = [32, 32, 32, 32, 32, 3]
+    return sum(2 * 9 * a * b for a, b in zip(cin, cout))
+
+
 def param_count():
     _declare()
     return int(lib().bm_net_param_count())

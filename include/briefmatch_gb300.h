@@ -198,9 +198,10 @@ bm_status bm_set_rng_position(bm_ctx* ctx, uint64_t calls);
  * processes one pair at a time).  Every pair is computed exactly as a fresh context
  * would compute it (bm_create, then bm_frame on its first and second frame); all
  * pairs must share N, iterations, jfMax, doubleProp, filter and the random stream.
- * Each stage runs as one launch over the union of all pairs' tiles; the matching
- * phase can run as one persistent cooperative launch with bounded grid barriers; a
- * whole step can be captured in a CUDA graph.  Frames and flows are packed in pair
+ * Each stage runs either as one launch over the union of all pairs' tiles or as
+ * one launch per pair (bm_batch_schedule.per_pair); the matching phase can run as one
+ * persistent cooperative launch with bounded grid barriers; a whole step can be
+ * captured in a CUDA graph.  Frames and flows are packed in pair
  * order: frames = pair0 frame0, pair0 frame1, pair1 frame0, ... (uint8, sx_in*sy_in
  * each); flows = pair0 U, pair0 V, pair1 U, ... (float). */
 typedef struct bm_batch bm_batch;
@@ -241,6 +242,16 @@ uint64_t bm_batch_launch_count(const bm_batch* b);
  * without timing, a new one is appended.  report receives a one-line summary. */
 bm_status bm_batch_autotune(bm_batch* b, const char* cache_path, int reps, char* report, size_t report_len);
 
+/* Seed every pair's matching with a proposal network (NULL detaches), as
+ * bm_set_proposal does for a context: per pair, the network on its two frames, the
+ * seeded initialisation, then `iterations` rounds with jump-flood maximum jfMax (0
+ * keeps the batch's).  Pair i's result equals a fresh context with the same proposal
+ * attached.  The batch switches to, and keeps, the per-pair schedule; the network
+ * must have been created for the largest pair's (sx_in/4) x (sy_in/4) and must not be
+ * used on another stream while the batch runs. */
+typedef struct bm_net bm_net;
+bm_status bm_batch_set_proposal(bm_batch* b, bm_net* net, float conf_threshold, uint32_t iterations, uint32_t jfMax);
+
 /* Self-test of the bounded grid barrier: `blocks` co-resident blocks wait for `expect`
  * arrivals for at most spin_limit polls each.  With expect > blocks nobody can pass:
  * every block gives up, *timed_out is set and BM_ERR_TIMEOUT returned. */
@@ -253,7 +264,6 @@ bm_status bm_selftest_barrier(uint32_t blocks, uint32_t expect, uint64_t spin_li
  * and activations with FP32 accumulation on the tensor cores, predicting the flow
  * (quarter-resolution pixels) and a confidence logit per quarter-resolution pixel.
  * Parameters are one FP32 vector: for each layer W[cout][9][cin] then b[cout]. */
-typedef struct bm_net bm_net;
 size_t bm_net_param_count(void);
 bm_status bm_net_create(uint32_t max_batch, uint32_t max_h4, uint32_t max_w4, bm_net** out);
 bm_status bm_net_destroy(bm_net* n);
@@ -276,7 +286,9 @@ bm_status bm_net_train_step(bm_net* n, uint32_t B, uint32_t h, uint32_t w, const
  * matches a pair runs the network on the previous and current frames and initialises
  * matching by bm_seed's rule, then runs `iterations` rounds with jump-flood maximum
  * jfMax (0 keeps the context's).  The network must have been created for at least
- * one image of (sx_in/4) x (sy_in/4). */
+ * one image of (sx_in/4) x (sy_in/4).  The network's buffers are used on the
+ * context's stream: one network may serve several contexts only if their work is
+ * serialised (same stream, or the caller orders the streams). */
 bm_status bm_set_proposal(bm_ctx* ctx, bm_net* net, float conf_threshold, uint32_t iterations, uint32_t jfMax);
 
 /* Seeded initialisation (the stage entry point): each up-sampled pixel first takes

@@ -159,16 +159,47 @@ def test_detached_proposal_is_plain():
     assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
 
 
+def test_batch_seeded_equals_single_contexts():
+    """A batch with a proposal attached gives, for every pair of uneven size, what a
+    fresh context with the same proposal attached gives."""
+    sizes = [(96, 64), (120, 72), (72, 56)]
+    params = [small_params(w, h, 2.0, 2.0, N=64) for w, h in sizes]
+    frames = [synth.make_pair(60 + k, w, h, 5.0)[:2] for k, (w, h) in enumerate(sizes)]
+    net = _net_with_spread_logits(max(h for _, h in sizes) // 4, max(w for w, _ in sizes) // 4)
+    want = []
+    for p, (f0, f1) in zip(params, frames):
+        eng = bm.FlowEngine(p)
+        bm.set_proposal(eng, net, 0.5, 1, 8)
+        eng.process_frame(f0)
+        want.append(eng.process_frame(f1))
+        eng.clean()
+    b = bm.Batch(params)
+    b.set_proposal(net, 0.5, 1, 8)
+    with pytest.raises(bm.BriefMatchException):
+        b.set_schedule(per_pair=0)
+    for use_graph in (0, 1):
+        b.set_schedule(per_pair=1, use_graph=use_graph)
+        b.load_frames(b.pack_frames(frames))
+        b.run()
+        b.synchronize()
+        for k, ((gu, gv), (wu, wv)) in enumerate(zip(b.read_flows(), want)):
+            assert np.array_equal(gu, wu) and np.array_equal(gv, wv), (use_graph, k)
+    b.close()
+
+
 def test_training_on_engine_flows_reduces_loss():
     """A short run of the training loop on BriefMatch's own flows for a few pairs:
     the held-in loss falls and the proposal moves toward BriefMatch's flow."""
     n = 24
     f0, f1, tgt, gt = learn.build_set(torch, n, target_iterations=2, chunk=n, workers=4)
     net = ProposalNet(8, learn.TRAIN_H // 4, learn.TRAIN_W // 4)
+    probe = range(8)
+    l_before = learn.batch_loss(torch, net, f0, f1, tgt, probe)
     e_before, _, _ = learn.score(torch, net, f0, f1, tgt, gt, range(4))
-    hist = learn.train_net(torch, net, f0, f1, tgt, np.arange(n), epochs=20, batch=8, lr=3e-3, log=None)
+    learn.train_net(torch, net, f0, f1, tgt, np.arange(n), epochs=20, batch=8, lr=3e-3, log=None)
+    l_after = learn.batch_loss(torch, net, f0, f1, tgt, probe)
     e_after, _, _ = learn.score(torch, net, f0, f1, tgt, gt, range(4))
-    assert hist[-1][1] < 0.7 * hist[0][1], hist
+    assert l_after[0] < 0.8 * l_before[0], (l_before, l_after)
     assert e_after < e_before, (e_before, e_after)
 
 
