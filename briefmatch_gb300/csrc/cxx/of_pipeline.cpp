@@ -116,7 +116,8 @@ std::string format_frame(const std::string& pattern, unsigned int frame)
 OFPipeline::OFPipeline()
     : m_doWriteMOT(false), m_doWriteFLO(false), m_doWriteLDR(false), m_verbose(false), m_doPrintError(false),
       m_endFrame(0), m_frame(0), m_stepFrame(1), m_startFrame(0), m_sx(0), m_sy(0), m_sx_in(0), m_sy_in(0), m_c(0),
-      m_rng("xorwow"), m_seed(0), m_bm(nullptr), m_bmP(nullptr), m_first(true)
+      m_rng("xorwow"), m_seed(0), m_propIterations(2), m_propJfMax(64), m_net(nullptr), m_bm(nullptr),
+      m_bmP(nullptr), m_first(true)
 {
 }
 
@@ -125,6 +126,8 @@ OFPipeline::~OFPipeline() { clear(); }
 void OFPipeline::clear()
 {
     delete m_bm;
+    if (m_net) bm_net_destroy(m_net);
+    m_net = nullptr;
     delete m_bmP;
     m_bm = nullptr;
     m_bmP = nullptr;
@@ -166,6 +169,10 @@ bool OFPipeline::setParams(int argc, char* argv[])
     args.str(&m_rng, "--random-stream", "-rng", "Random search stream: xorwow (the reference's) or philox");
     unsigned int seed = 0;
     args.uint(&seed, "--pattern-seed", "-ps", "Seed of the BRIEF sampling pattern", 0u, 4294967295u);
+    args.str(&m_proposal, "--proposal", "-pn", "Learned proposal weights (float32 file) seeding the matching");
+    args.uint(&m_propIterations, "--proposal-iterations", "-pit", "Iterations when seeded by the proposal", 0u, 100u);
+    args.uint(&m_propJfMax, "--proposal-jf-max", "-pjm", "Max jump-flooding distance when seeded by the proposal", 1u,
+              10000u);
     if (!args.read(argc, argv)) return false;
     m_seed = seed;
     if (m_rng != "xorwow" && m_rng != "philox")
@@ -235,6 +242,23 @@ void OFPipeline::setup()
     bm_get_params(m_bm->context(), &p);
     bm_throw_on_error(bm_make_pattern(&p, m_seed, pattern.data()));
     m_bm->setPattern(pattern);
+    if (!m_proposal.empty()) {
+        // engine extension: seed every pair's matching with the learned proposal
+        std::FILE* f = std::fopen(m_proposal.c_str(), "rb");
+        if (!f) throw BriefMatchException("Cannot read proposal weights '" + m_proposal + "'");
+        std::vector<float> w(bm_net_param_count());
+        const size_t got = std::fread(w.data(), sizeof(float), w.size(), f);
+        const bool extra = std::fgetc(f) != EOF;
+        std::fclose(f);
+        if (got != w.size() || extra)
+            throw BriefMatchException("Proposal weights '" + m_proposal + "' do not hold " +
+                                      std::to_string(w.size()) + " float32 parameters");
+        bm_throw_on_error(bm_net_create(1, m_sy_in / 4, m_sx_in / 4, &m_net));
+        bm_throw_on_error(bm_net_set_params(m_net, w.data(), w.size()));
+        bm_throw_on_error(bm_set_proposal(m_bm->context(), m_net, 0.5f, m_propIterations, m_propJfMax));
+        std::fprintf(stderr, "Proposal:                %s (%u iterations, jump-flooding max %u)\n\n",
+                     m_proposal.c_str(), m_propIterations, m_propJfMax);
+    }
     m_frameData.resize((size_t)m_sx_in * m_sy_in);
     m_first = true;
 }

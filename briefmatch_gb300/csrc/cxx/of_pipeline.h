@@ -27,8 +27,10 @@ private:
 
     bool m_doWriteMOT, m_doWriteFLO, m_doWriteLDR, m_verbose, m_doPrintError;
     unsigned int m_endFrame, m_frame, m_stepFrame, m_startFrame, m_sx, m_sy, m_sx_in, m_sy_in, m_c;
-    std::string m_input, m_flowGT, m_output, m_rng;
+    std::string m_input, m_flowGT, m_output, m_rng, m_proposal;
     unsigned long long m_seed;
+    unsigned int m_propIterations, m_propJfMax;
+    bm_net* m_net;
     BriefMatch* m_bm;
     BMParams* m_bmP;
     std::vector<unsigned char> m_frameData;

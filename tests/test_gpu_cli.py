@@ -59,3 +59,26 @@ def test_cli_bin_png_and_epe(tmp_path):
     run("-i", str(tmp_path / "f%02d.png"), "-f", "0:1", "-o", str(tmp_path / "c%02d.png"), "-mm", "5")
     rgb = read_png_rgb(str(tmp_path / "c01.png"))
     assert rgb.shape == (H, W, 3) and rgb.std() > 0
+
+
+def test_cli_proposal_matches_library(tmp_path):
+    """--proposal seeds every pair with the learned proposal, as bm_set_proposal does."""
+    from briefmatch_gb300 import learn
+
+    W, H = 120, 80
+    frames, _ = synth.make_sequence(5, W, H, 3, vmax=6.0)
+    for k, f in enumerate(frames):
+        write_pgm(str(tmp_path / ("f%02d.pgm" % k)), f)
+    run("-i", str(tmp_path / "f%02d.pgm"), "-f", "0:2", "-o", str(tmp_path / "o%02d.flo"), "-ux", "2", "-uy", "2",
+        "-fl", "64", "--proposal", learn.DEFAULT_WEIGHTS, "-pit", "1", "-pjm", "8")
+    prm = bm.BMParams.derive(W, H, 2.0, 2.0, N=64)
+    eng = bm.FlowEngine(prm)
+    net = learn.load_net(learn.DEFAULT_WEIGHTS, 1, H // 4, W // 4)
+    bm.set_proposal(eng, net, 0.5, 1, 8)
+    for k, f in enumerate(frames):
+        u, v = eng.process_frame(f)
+        fu, fv = read_flo(str(tmp_path / ("o%02d.flo" % k)))
+        assert np.array_equal(fu, u) and np.array_equal(fv, v), k
+    eng.clean()
+    with pytest.raises(AssertionError):
+        run("-i", str(tmp_path / "f%02d.pgm"), "-f", "0:1", "--proposal", str(tmp_path / "f00.pgm"))
