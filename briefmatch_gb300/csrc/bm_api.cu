@@ -495,7 +495,11 @@ bm_status bm_get_params(const bm_ctx* c, bm_params* out)
 bm_status bm_set_stream(bm_ctx* c, void* stream)
 {
     if (check_ctx(c)) return BM_ERR_INVALID;
-    c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+    const cudaStream_t s = stream ? (cudaStream_t)stream : c->own_stream;
+    // work already queued on the old stream (buffer clears, pattern upload, frames)
+    // finishes before anything queued on the new one
+    if (s != c->stream) BM_CUDA(cudaStreamSynchronize(c->stream));
+    c->stream = s;
     return BM_OK;
 }
 

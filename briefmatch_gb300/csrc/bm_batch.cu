@@ -899,7 +899,11 @@ bm_status bm_batch_set_stream(bm_batch* b, void* stream)
 {
     if (!b) return bfail(BM_ERR_INVALID, "null batch");
     cudaStream_t s = stream ? (cudaStream_t)stream : b->own_stream;
-    if (s != b->stream) destroy_graph(b);
+    if (s != b->stream) {
+        // work already queued on the old stream finishes before the new one's
+        BB_CUDA(cudaStreamSynchronize(b->stream));
+        destroy_graph(b);
+    }
     b->stream = s;
     return BM_OK;
 }

@@ -504,10 +504,13 @@ __device__ __forceinline__ void median_px(const float* __restrict__ in, float* _
 // used four times and every arithmetic instruction serves two outputs.  The
 // (2s + TX) x (2s + TRI_BY) neighbourhood is staged in shared memory with
 // clamp-to-edge addressing.  The three Gaussians are one exp2 of the summed
-// exponents: with kE = sqrt(cE) and kI = sqrt(cI), each scaled difference is one
-// FMA against the centre's negated scaled value (kE*u - kE*uc), the squared terms
-// accumulate by FMA onto the row term j^2*cS, and exp2 takes the negated sum --
-// six FP32 operations per tap and output before the three accumulations.  The
+// exponents cE*(du^2 + dv^2) + cI*dI^2 + cS*j^2 = r*(du'^2 + dv'^2 + dI'^2 + j^2*cS/r)
+// with du' = kE*u - kE*uc: kE is the power of two nearest sqrt(cE) (so kE*uc is
+// exact and du' is the scaled difference rounded once -- a rounded centre would
+// tilt every weight of the window the same way), r = cE/kE^2, kI = sqrt(cI/r).
+// Each scaled difference is one FMA against the centre's negated scaled value, the
+// squared terms accumulate by FMA onto the row term, one multiply by r, one exp2:
+// seven FP32 operations per tap and output before the three accumulations.  The
 // column factor exp2(-cS*i^2) is applied once per column (the inner loop runs down
 // a column); row terms outside the window are +inf (weight 0).
 // `smem` must hold tri_smem_bytes(s).
@@ -536,6 +539,9 @@ __device__ __forceinline__ void trilateral_block(const float* __restrict__ U, co
     float* sI = reinterpret_cast<float*>(suv + TW * TH);
     const int x0 = bx0 - s, y0 = by0 - s;
     const int tid = threadIdx.y * TX + threadIdx.x;
+    // kE: the power of two nearest sqrt(cE) (exact scaling), r_ the remaining factor
+    const float kE = exp2f(rintf(0.5f * __log2f(cE))), r_ = cE / (kE * kE);
+    const float kI = sqrtf(cI / r_), cS_r = cS / r_;
     for (int k = tid; k < TW * TH; k += TX * TRI_TY) {
         const int r = k / TW, c = k - r * TW;
         const int gx = min(sx - 1, max(0, x0 + c)), gy = min(sy - 1, max(0, y0 + r));
@@ -548,7 +554,7 @@ __device__ __forceinline__ void trilateral_block(const float* __restrict__ U, co
 #pragma unroll
         for (int r = 0; r < TRI_R; r++) {
             const int j = m - r - s;  // vertical offset of this source row for output r
-            t[r] = (j >= -s && j < s) ? (float)(j * j) * cS : __int_as_float(0x7f800000);
+            t[r] = (j >= -s && j < s) ? (float)(j * j) * cS_r : __int_as_float(0x7f800000);
         }
         rowf[m] = make_float4(t[0], t[1], t[2], t[3]);
     }
@@ -557,7 +563,6 @@ __device__ __forceinline__ void trilateral_block(const float* __restrict__ U, co
     const int x = bx0 + threadIdx.x;
     const int yb = by0 + threadIdx.y * TRI_R;
     if (x >= sx || yb >= sy) return;
-    const float kE = sqrtf(cE), kI = sqrtf(cI);
     float umc[TRI_R], vmc[TRI_R], Ic[TRI_R];
 #pragma unroll
     for (int r = 0; r < TRI_R; r++) {
@@ -570,7 +575,7 @@ __device__ __forceinline__ void trilateral_block(const float* __restrict__ U, co
     const f2x umA = pk2(umc[0], umc[1]), umB = pk2(umc[2], umc[3]);
     const f2x vmA = pk2(vmc[0], vmc[1]), vmB = pk2(vmc[2], vmc[3]);
     const f2x IA = pk2(Ic[0], Ic[1]), IB = pk2(Ic[2], Ic[3]);
-    const f2x kEE = pk2(kE, kE), kII = pk2(kI, kI);
+    const f2x kEE = pk2(kE, kE), kII = pk2(kI, kI), rr = pk2(r_, r_);
     f2x ufA = 0, ufB = 0, vfA = 0, vfB = 0, WA = 0, WB = 0;  // 0 bits = (0.0f, 0.0f)
     const int row0 = threadIdx.y * TRI_R;
     for (int i = -s; i < s; i++) {
@@ -585,7 +590,7 @@ __device__ __forceinline__ void trilateral_block(const float* __restrict__ U, co
             const f2x uu = pk2(uv.x, uv.x), vv = pk2(uv.y, uv.y), ii = pk2(i1, i1);
             f2x du = fma2(uu, kEE, umA), dv = fma2(vv, kEE, vmA), dI = fma2(ii, kII, IA);
             f2x q = fma2(dI, dI, fma2(dv, dv, fma2(du, du, pk2(rf.x, rf.y))));
-            f2x w = ex2n_2(q);
+            f2x w = ex2n_2(mul2(q, rr));
             cuA = fma2(w, uu, cuA);
             cvA = fma2(w, vv, cvA);
             cwA = add2(cwA, w);
@@ -593,7 +598,7 @@ __device__ __forceinline__ void trilateral_block(const float* __restrict__ U, co
             dv = fma2(vv, kEE, vmB);
             dI = fma2(ii, kII, IB);
             q = fma2(dI, dI, fma2(dv, dv, fma2(du, du, pk2(rf.z, rf.w))));
-            w = ex2n_2(q);
+            w = ex2n_2(mul2(q, rr));
             cuB = fma2(w, uu, cuB);
             cvB = fma2(w, vv, cvB);
             cwB = add2(cwB, w);

@@ -505,7 +505,10 @@ bm_status bm_net_create(uint32_t max_batch, uint32_t max_h4, uint32_t max_w4, bm
         const double bound = std::sqrt(6.0 / (9.0 * CIN_R[l])) * (l == NL - 1 ? 0.1 : 1.0);
         for (size_t k = 0; k < layer_w_count(l); k++) p[n->poff[l] + k] = (float)((2 * uni() - 1) * bound);
     }
-    if (cudaMemcpy(n->d_master, p.data(), off * 4, cudaMemcpyHostToDevice) != cudaSuccess) {
+    // the clears and the upload run on the legacy stream; finish them before the
+    // caller's streams (possibly non-blocking) use the buffers
+    if (cudaMemcpy(n->d_master, p.data(), off * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaStreamSynchronize(cudaStreamLegacy) != cudaSuccess) {
         bm_net_destroy(n);
         return nfail(BM_ERR_CUDA, "bm_net_create: parameter upload failed");
     }
@@ -534,6 +537,7 @@ bm_status bm_net_set_params(bm_net* n, const float* h_params, size_t count)
     BN_CUDA(cudaMemcpy(n->d_master, h_params, count * 4, cudaMemcpyHostToDevice));
     BN_CUDA(cudaMemset(n->d_m, 0, count * 4));
     BN_CUDA(cudaMemset(n->d_v, 0, count * 4));
+    BN_CUDA(cudaStreamSynchronize(cudaStreamLegacy));  // see bm_net_create
     n->step = 0;
     n->packed = false;
     return BM_OK;

@@ -116,7 +116,8 @@ bm_status bm_destroy(bm_ctx* ctx);
 /* BriefMatch::getParams, briefmatch.h:118 (P is the derived tap count). */
 bm_status bm_get_params(const bm_ctx* ctx, bm_params* out);
 
-/* Queue subsequent work on this cudaStream_t (NULL = the context's own stream). */
+/* Queue subsequent work on this cudaStream_t (NULL = the context's own stream).
+ * Switching to another stream first waits for the work queued on the old one. */
 bm_status bm_set_stream(bm_ctx* ctx, void* stream);
 bm_status bm_synchronize(bm_ctx* ctx);
 
