@@ -47,10 +47,24 @@ sys.path.insert(0, ROOT)
 
 METRIC = "output flow Mpx/s at fixed EPE: batched+learned-seeded vs plain, same GB300"
 UNIT = "Mpx/s"
-W, H, FRAMES, UP, NBITS, VMAX, SEED = 1024, 436, 8, 2.9, 128, 15.0, 20261203
-PAIRS = FRAMES - 1
-WORKLOAD = ("%s engine, synthetic 1024x436 8-bit sequence of 8 frames (7 pairs, |v|<=15 px), "
-            "up-sampling 2.9x2.9, feature_length 128, temporal init, FP32 flow out")
+# the workload configurations: width, height, frames per sequence, up-sampling,
+# feature_length, max |v|.  "2" is the one the metric is quoted on (the default);
+# "1" and "3" are the reference's small case and the 1920x1080 u4.9 N512 stress case,
+# timed beside the reference's own kernels with --config.
+CONFIGS = {"1": (584, 388, 2, 1.5, 32, 10.0), "2": (1024, 436, 8, 2.9, 128, 15.0), "3": (1920, 1080, 5, 4.9, 512, 24.0)}
+SEED = 20261203
+
+
+def set_config(name):
+    global W, H, FRAMES, UP, NBITS, VMAX, PAIRS, WORKLOAD
+    W, H, FRAMES, UP, NBITS, VMAX = CONFIGS[name]
+    PAIRS = FRAMES - 1
+    WORKLOAD = ("%%s engine, synthetic %dx%d 8-bit sequence of %d frames (%d pair%s, |v|<=%g px), "
+                "up-sampling %gx%g, feature_length %d, temporal init, FP32 flow out"
+                % (W, H, FRAMES, PAIRS, "s" if PAIRS > 1 else "", VMAX, UP, UP, NBITS))
+
+
+set_config("2")
 
 
 def parse():
@@ -64,6 +78,10 @@ def parse():
     ap.add_argument("--no-batched", action="store_true", help="skip the 64-pair batched workload")
     ap.add_argument("--batch-pairs", type=int, default=64)
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-seeded engine")
+    ap.add_argument("--config", default="2", choices=sorted(CONFIGS),
+                    help="workload: 1 = 584x388 u1.5 N32 pair, 2 = 1024x436 u2.9 N128 8-frame sequence (default), "
+                         "3 = 1920x1080 u4.9 N512 5-frame sequence; 1 and 3 run the plain engine beside the "
+                         "reference's own kernels")
     ap.add_argument("--schedule", default=None,
                     help="ITERATIONS/JFMAX for the learned-seeded engine instead of choosing it by calibration")
     return ap.parse_args()
@@ -480,6 +498,11 @@ def run_engine(args, torch, world, rank):
         "cpu_baseline": cpu,
         "batched": batched,
     }
+    if args.config != "2" and rank == 0 and world == 1:
+        try:
+            line["reference_cuda_build"] = reference_cuda(torch, prm, pattern, frames, args)
+        except Exception as e:  # the reference kernel build is optional
+            line["reference_cuda_build"] = {"unavailable": str(e)[:200]}
     if rank == 0:
         print(json.dumps(line), flush=True)
     plain.clean()
@@ -729,6 +752,9 @@ def reference_cuda(torch, prm, pattern, frames, args):
 
 def main():
     args = parse()
+    set_config(args.config)
+    if args.config != "2":
+        args.no_learned = args.no_batched = args.no_cpu_baseline = True
     import torch
 
     world, rank = dist_init(torch)
