@@ -396,7 +396,7 @@ class FlowEngine(BriefMatch):
 class bm_batch_schedule(ctypes.Structure):
     _fields_ = [("persistent", ctypes.c_uint32), ("blocks_per_sm", ctypes.c_uint32), ("snake", ctypes.c_uint32),
                 ("use_graph", ctypes.c_uint32), ("spin_limit", ctypes.c_uint64), ("wave_bytes", ctypes.c_uint64),
-                ("per_pair", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+                ("per_pair", ctypes.c_uint32), ("streams", ctypes.c_uint32)]
 
 
 class Batch:

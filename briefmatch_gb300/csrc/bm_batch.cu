@@ -312,6 +312,14 @@ struct bm_batch {
     float net_logit_min = 0.0f;
     uint32_t net_iterations = 0, net_jfMax = 0;
     float* d_pred = nullptr;   // [h4][w4][3] of the pair being seeded (pairs run in stream order)
+    // concurrent branches of the per-pair schedule (bm_batch_schedule.streams):
+    // streams forked from and joined back into the batch stream, and for a proposal
+    // one network copy and prediction buffer per extra branch
+    std::vector<cudaStream_t> branch;
+    std::vector<cudaEvent_t> branch_done;
+    cudaEvent_t fork_ev = nullptr;
+    std::vector<bm_net*> net_copy;
+    std::vector<float*> pred_copy;
 };
 
 namespace {
@@ -395,10 +403,9 @@ bm_status enqueue_step(bm_batch* b, const bm_batch_schedule& s)
 
 // One pair through the single-pair kernels (parameters in the launch, as a plain
 // context runs it), into the batch's buffers.
-bm_status enqueue_pair(bm_batch* b, const bm_batch_schedule& s, int j)
+bm_status enqueue_pair(bm_batch* b, const bm_batch_schedule& s, int j, cudaStream_t st, bm_net* net, float* d_pred)
 {
     const PairDev& d = b->pairs[j];
-    cudaStream_t st = b->stream;
     const size_t ni = (size_t)d.sx_in * d.sy_in;
     const bool resample = d.sx != d.sx_in || d.sy != d.sy_in;
     BB_CUDA(u8_to_f32(d.frame[0], d.guide, ni, st));
@@ -415,14 +422,14 @@ bm_status enqueue_pair(bm_batch* b, const bm_batch_schedule& s, int j)
     }
     int cur = 0;
     uint32_t iterations = b->iterations, jfMax = b->jfMax;
-    if (b->net) {
+    if (net) {
         // the proposal for this pair, then the seeded initialisation (bm_seed's rule)
         const uint32_t w4 = (uint32_t)d.sx_in / 4, h4 = (uint32_t)d.sy_in / 4;
-        bm_status nst = bm_net_prepare(b->net, 0, d.frame[0], d.frame[1], (uint32_t)d.sx_in, (uint32_t)d.sy_in, st);
-        if (nst == BM_OK) nst = bm_net_forward(b->net, 1, h4, w4, b->d_pred, st);
+        bm_status nst = bm_net_prepare(net, 0, d.frame[0], d.frame[1], (uint32_t)d.sx_in, (uint32_t)d.sy_in, st);
+        if (nst == BM_OK) nst = bm_net_forward(net, 1, h4, w4, d_pred, st);
         if (nst != BM_OK) return nst;
         const float scx = 4.0f * (float)d.sx / (float)d.sx_in, scy = 4.0f * (float)d.sy / (float)d.sy_in;
-        BB_CUDA(seed_field(d.F[0], d.F[1], d.flow[cur], d.flow[cur ^ 1], d.cost, d.sx, d.sy, (int)b->nsp, 1, b->d_pred,
+        BB_CUDA(seed_field(d.F[0], d.F[1], d.flow[cur], d.flow[cur ^ 1], d.cost, d.sx, d.sy, (int)b->nsp, 1, d_pred,
                            (int)w4, (int)h4, scx, scy, b->net_logit_min, st));
         iterations = b->net_iterations;
         if (b->net_jfMax) jfMax = b->net_jfMax;
@@ -457,21 +464,58 @@ bm_status enqueue_pair(bm_batch* b, const bm_batch_schedule& s, int j)
     } else {
         BB_CUDA(flow_to_planes(d.flow[cur], d.flow_in, d.flow_in + ni, ni, st));
     }
-    b->launches += 6 + (uint64_t)iterations * levels - (b->net ? 1 : 0);
+    b->launches += 6 + (uint64_t)iterations * levels - (net ? 1 : 0);
     return BM_OK;
 }
 
 bm_status enqueue_refine(bm_batch* b, int lo, int hi);
+bm_status enqueue_refine_pair(bm_batch* b, int j, cudaStream_t st);
 
-bm_status enqueue_wave(bm_batch* b, const bm_batch_schedule& s, int lo, int hi)
+// The per-pair schedule over pairs [lo, hi).  With k > 1 streams the pairs are
+// dealt to k branches (largest first, each to the branch with the least work so
+// far) that fork from the batch stream and join back into it; each pair's whole
+// pipeline, refinement included, stays on its branch.
+bm_status enqueue_per_pair(bm_batch* b, const bm_batch_schedule& s, int lo, int hi)
 {
-    if (s.per_pair) {
+    const int k = std::min<int>((int)s.streams, (int)b->branch.size() + 1);
+    if (k <= 1) {
         for (int j = lo; j < hi; j++) {
-            bm_status st = enqueue_pair(b, s, j);
+            bm_status st = enqueue_pair(b, s, j, b->stream, b->net, b->d_pred);
             if (st != BM_OK) return st;
         }
         return enqueue_refine(b, lo, hi);
     }
+    std::vector<cudaStream_t> bs(k);
+    bs[0] = b->stream;
+    for (int i = 1; i < k; i++) bs[i] = b->branch[i - 1];
+    BB_CUDA(cudaEventRecord(b->fork_ev, b->stream));
+    for (int i = 1; i < k; i++) BB_CUDA(cudaStreamWaitEvent(bs[i], b->fork_ev, 0));
+    std::vector<uint64_t> load(k, 0);
+    std::vector<std::vector<int>> deal(k);
+    for (int j = hi - 1; j >= lo; j--) {
+        const int i = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        load[i] += b->ws[j];
+        deal[i].push_back(j);
+    }
+    for (int i = 0; i < k; i++) {
+        bm_net* net = b->net ? (i == 0 ? b->net : b->net_copy[i - 1]) : nullptr;
+        float* pred = i == 0 ? b->d_pred : (b->net ? b->pred_copy[i - 1] : nullptr);
+        for (int j : deal[i]) {
+            bm_status st = enqueue_pair(b, s, j, bs[i], net, pred);
+            if (st == BM_OK) st = enqueue_refine_pair(b, j, bs[i]);
+            if (st != BM_OK) return st;
+        }
+    }
+    for (int i = 1; i < k; i++) {
+        BB_CUDA(cudaEventRecord(b->branch_done[i - 1], bs[i]));
+        BB_CUDA(cudaStreamWaitEvent(b->stream, b->branch_done[i - 1], 0));
+    }
+    return BM_OK;
+}
+
+bm_status enqueue_wave(bm_batch* b, const bm_batch_schedule& s, int lo, int hi)
+{
+    if (s.per_pair) return enqueue_per_pair(b, s, lo, hi);
     const BatchDev bd = batch_dev(b, lo, hi);
     const unsigned int t_up = b->pre_up[hi] - b->pre_up[lo], t_in = b->pre_in[hi] - b->pre_in[lo];
     cudaStream_t st = b->stream;
@@ -560,26 +604,85 @@ bm_status enqueue_wave(bm_batch* b, const bm_batch_schedule& s, int lo, int hi)
 
 // Refinement: one launch per pair and stage, each sized to its pair (median window,
 // trilateral window and shared memory).
+bm_status enqueue_refine_pair(bm_batch* b, int j, cudaStream_t st)
+{
+    const PairDev& d = b->pairs[j];
+    const bm_params& p = b->prm[b->order[j]];
+    const size_t ni = (size_t)d.sx_in * d.sy_in;
+    if (b->filter) {
+        const int fs = d.fsize == 0 ? 1 : d.fsize;
+        BB_CUDA(median_pass(d.flow_in, d.flow_in + ni, d.tmp, d.tmp + ni, 1, fs, d.sx_in, d.sy_in, st));
+        BB_CUDA(median_pass(d.tmp, d.tmp + ni, d.flow_med, d.flow_med + ni, 0, fs, d.sx_in, d.sy_in, st));
+        BB_CUDA(trilateral(d.flow_in, d.flow_in + ni, d.flow_med, d.flow_med + ni, d.guide, d.flow_out,
+                           d.flow_out + ni, d.sx_in, d.sy_in, d.tri_s, p.sEPE * p.sEPE, p.sI * p.sI, p.sS * p.sS,
+                           st));
+        b->launches += 3;
+    } else {
+        BB_CUDA(cudaMemcpyAsync(d.flow_out, d.flow_in, 2 * ni * sizeof(float), cudaMemcpyDeviceToDevice, st));
+    }
+    return BM_OK;
+}
+
 bm_status enqueue_refine(bm_batch* b, int lo, int hi)
 {
-    cudaStream_t st = b->stream;
     for (int j = lo; j < hi; j++) {
-        const PairDev& d = b->pairs[j];
-        const bm_params& p = b->prm[b->order[j]];
-        const size_t ni = (size_t)d.sx_in * d.sy_in;
-        if (b->filter) {
-            const int fs = d.fsize == 0 ? 1 : d.fsize;
-            BB_CUDA(median_pass(d.flow_in, d.flow_in + ni, d.tmp, d.tmp + ni, 1, fs, d.sx_in, d.sy_in, st));
-            BB_CUDA(median_pass(d.tmp, d.tmp + ni, d.flow_med, d.flow_med + ni, 0, fs, d.sx_in, d.sy_in, st));
-            BB_CUDA(trilateral(d.flow_in, d.flow_in + ni, d.flow_med, d.flow_med + ni, d.guide, d.flow_out,
-                               d.flow_out + ni, d.sx_in, d.sy_in, d.tri_s, p.sEPE * p.sEPE, p.sI * p.sI,
-                               p.sS * p.sS, st));
-            b->launches += 3;
-        } else {
-            BB_CUDA(cudaMemcpyAsync(d.flow_out, d.flow_in, 2 * ni * sizeof(float), cudaMemcpyDeviceToDevice, st));
+        bm_status st = enqueue_refine_pair(b, j, b->stream);
+        if (st != BM_OK) return st;
+    }
+    return BM_OK;
+}
+
+// Branch streams, events and (with a proposal) network copies for k - 1 extra
+// branches; created outside any capture.
+bm_status ensure_branches(bm_batch* b, int k)
+{
+    if (k > 8) return bfail(BM_ERR_LIMIT, "bm_batch: at most 8 concurrent streams");
+    if (!b->fork_ev) BB_CUDA(cudaEventCreateWithFlags(&b->fork_ev, cudaEventDisableTiming));
+    while ((int)b->branch.size() < k - 1) {
+        cudaStream_t st = nullptr;
+        cudaEvent_t ev = nullptr;
+        BB_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        b->branch.push_back(st);
+        BB_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        b->branch_done.push_back(ev);
+    }
+    if (b->net) {
+        size_t cells = 0;
+        uint32_t mh = 0, mw = 0;
+        for (const auto& p : b->prm) {
+            cells = std::max(cells, (size_t)(p.sx_in / 4) * (p.sy_in / 4));
+            mh = std::max(mh, p.sy_in / 4);
+            mw = std::max(mw, p.sx_in / 4);
+        }
+        std::vector<float> params(bm_net_param_count());
+        if ((int)b->net_copy.size() < k - 1) {
+            bm_status st = bm_net_get_params(b->net, params.data(), params.size());
+            if (st != BM_OK) return st;
+        }
+        while ((int)b->net_copy.size() < k - 1) {
+            bm_net* n = nullptr;
+            bm_status st = bm_net_create(1, mh, mw, &n);
+            if (st == BM_OK) st = bm_net_set_params(n, params.data(), params.size());
+            if (st != BM_OK) {
+                if (n) bm_net_destroy(n);
+                return st;
+            }
+            b->net_copy.push_back(n);
+            float* pr = nullptr;
+            if (cudaMalloc((void**)&pr, cells * 3 * sizeof(float)) != cudaSuccess)
+                return bfail(BM_ERR_NOMEM, "bm_batch: prediction buffer allocation failed");
+            b->pred_copy.push_back(pr);
         }
     }
     return BM_OK;
+}
+
+void drop_net_copies(bm_batch* b)
+{
+    for (bm_net* n : b->net_copy) bm_net_destroy(n);
+    for (float* p : b->pred_copy) cudaFree(p);
+    b->net_copy.clear();
+    b->pred_copy.clear();
 }
 
 void destroy_graph(bm_batch* b)
@@ -888,6 +991,10 @@ bm_status bm_batch_destroy(bm_batch* b)
     if (b->d_pre) cudaFree(b->d_pre);
     if (b->d_sync) cudaFree(b->d_sync);
     if (b->d_pred) cudaFree(b->d_pred);
+    drop_net_copies(b);
+    for (cudaStream_t st : b->branch) cudaStreamDestroy(st);
+    for (cudaEvent_t ev : b->branch_done) cudaEventDestroy(ev);
+    if (b->fork_ev) cudaEventDestroy(b->fork_ev);
     if (b->own_stream) cudaStreamDestroy(b->own_stream);
     delete b;
     return BM_OK;
@@ -984,6 +1091,11 @@ bm_status bm_batch_set_schedule(bm_batch* b, const bm_batch_schedule* s)
     if (!b || !s) return bfail(BM_ERR_INVALID, "bm_batch_set_schedule: null argument");
     if (b->net && !s->per_pair)
         return bfail(BM_ERR_INVALID, "bm_batch_set_schedule: a batch with a proposal runs the per-pair schedule");
+    if (s->per_pair && s->streams > 1) {
+        if (b->stream) BB_CUDA(cudaStreamSynchronize(b->stream));
+        bm_status st = ensure_branches(b, (int)s->streams);
+        if (st != BM_OK) return st;
+    }
     b->sched = *s;
     if (b->sched.blocks_per_sm == 0 || (int)b->sched.blocks_per_sm > b->coop_blocks_per_sm)
         b->sched.blocks_per_sm = (uint32_t)b->coop_blocks_per_sm;
@@ -1039,11 +1151,14 @@ bm_status bm_batch_set_proposal(bm_batch* b, bm_net* net, float conf_threshold, 
         b->sched.per_pair = 1;
         b->sched.persistent = 0;
     }
+    if (b->stream) BB_CUDA(cudaStreamSynchronize(b->stream));
+    drop_net_copies(b);
     b->net = net;
     b->net_logit_min = net ? std::log(conf_threshold / (1.0f - conf_threshold)) : 0.0f;
     b->net_iterations = iterations;
     b->net_jfMax = jfMax;
     destroy_graph(b);
+    if (net && b->sched.streams > 1) return ensure_branches(b, (int)b->sched.streams);
     return BM_OK;
 }
 
@@ -1076,6 +1191,7 @@ bm_status bm_batch_autotune(bm_batch* b, const char* cache_path, int reps, char*
             ok &= grab("use_graph", v) && ((s.use_graph = (uint32_t)v), true);
             ok &= grab("wave_bytes", v) && ((s.wave_bytes = v), true);
             ok &= grab("per_pair", v) && ((s.per_pair = (uint32_t)v), true);
+            if (grab("streams", v)) s.streams = (uint32_t)v;
             if (ok) {
                 bm_batch_set_schedule(b, &s);
                 if (report) std::snprintf(report, report_len, "cached: %s", hit.c_str());
@@ -1095,7 +1211,13 @@ bm_status bm_batch_autotune(bm_batch* b, const char* cache_path, int reps, char*
         cands.push_back(s);
     }
     {
-        bm_batch_schedule s = cands.back();
+        const bm_batch_schedule base = cands.back();
+        for (uint32_t k : {2u, 4u}) {   // pairs on concurrent branches of the graph
+            bm_batch_schedule s = base;
+            s.streams = k;
+            cands.push_back(s);
+        }
+        bm_batch_schedule s = base;
         s.use_graph = 0;   // per-pair launches without the graph
         cands.push_back(s);
     }
@@ -1136,7 +1258,8 @@ bm_status bm_batch_autotune(bm_batch* b, const char* cache_path, int reps, char*
         float ms = 0;
         cudaEventElapsedTime(&ms, e0, e1);
         ms /= reps;
-        rep << "{per_pair=" << s.per_pair << ",persistent=" << s.persistent << ",wave=" << (s.wave_bytes >> 20) << "MB: "
+        rep << "{per_pair=" << s.per_pair << ",streams=" << (s.streams > 1 ? s.streams : 1) << ",graph=" << s.use_graph
+            << ",persistent=" << s.persistent << ",wave=" << (s.wave_bytes >> 20) << "MB: "
             << (st == BM_OK ? std::to_string(ms) : std::string("failed")) << " ms} ";
         if (st == BM_OK && ms < best_ms) {
             best_ms = ms;
@@ -1150,12 +1273,14 @@ bm_status bm_batch_autotune(bm_batch* b, const char* cache_path, int reps, char*
         std::ofstream out(cache_path, std::ios::app);
         out << "{\"key\": \"" << key << "\", \"persistent\": " << best.persistent << ", \"blocks_per_sm\": "
             << best.blocks_per_sm << ", \"snake\": " << best.snake << ", \"use_graph\": " << best.use_graph
-            << ", \"wave_bytes\": " << best.wave_bytes << ", \"per_pair\": " << best.per_pair << ", \"ms\": "
+            << ", \"wave_bytes\": " << best.wave_bytes << ", \"per_pair\": " << best.per_pair
+            << ", \"streams\": " << best.streams << ", \"ms\": "
             << best_ms << "}\n";
     }
     if (report)
-        std::snprintf(report, report_len, "%s-> per_pair=%u persistent=%u wave=%lluMB", rep.str().c_str(),
-                      best.per_pair, best.persistent, (unsigned long long)(best.wave_bytes >> 20));
+        std::snprintf(report, report_len, "%s-> per_pair=%u streams=%u graph=%u persistent=%u wave=%lluMB",
+                      rep.str().c_str(), best.per_pair, best.streams > 1 ? best.streams : 1, best.use_graph,
+                      best.persistent, (unsigned long long)(best.wave_bytes >> 20));
     return BM_OK;
 }
 

@@ -217,7 +217,10 @@ typedef struct bm_batch_schedule {
                                 (smallest pairs first, so a wave stays L2-resident); 0 = one wave */
     uint32_t per_pair;       /* every stage as a launch per pair (the single-pair kernels,
                                 parameters in the launch) instead of union-of-tiles launches */
-    uint32_t reserved;
+    uint32_t streams;        /* per-pair schedule: pairs dealt to this many concurrent streams
+                                forked from and joined back into the batch stream (0, 1 = one);
+                                with a proposal, each extra stream gets a copy of the network
+                                taken when the schedule or the proposal is set */
 } bm_batch_schedule;
 
 bm_status bm_batch_create(const bm_params* pairs, uint32_t count, bm_batch** out);

@@ -45,6 +45,9 @@ def _single(params, frames):
     dict(persistent=1, snake=1, use_graph=1, wave_bytes=3 << 20),    # small waves
     dict(per_pair=1, persistent=0, snake=1, use_graph=1),
     dict(per_pair=1, persistent=0, snake=0, use_graph=0),
+    dict(per_pair=1, persistent=0, snake=1, use_graph=1, streams=2),   # concurrent branches in the graph
+    dict(per_pair=1, persistent=0, snake=1, use_graph=0, streams=3),
+    dict(per_pair=1, persistent=0, snake=1, use_graph=1, streams=3, wave_bytes=3 << 20),
 ])
 def test_batch_equals_single_pairs(sched):
     params, frames = _batch_inputs()

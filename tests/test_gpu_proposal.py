@@ -177,8 +177,8 @@ def test_batch_seeded_equals_single_contexts():
     b.set_proposal(net, 0.5, 1, 8)
     with pytest.raises(bm.BriefMatchException):
         b.set_schedule(per_pair=0)
-    for use_graph in (0, 1):
-        b.set_schedule(per_pair=1, use_graph=use_graph)
+    for use_graph, streams in ((0, 1), (1, 1), (1, 2), (0, 3)):
+        b.set_schedule(per_pair=1, use_graph=use_graph, streams=streams)
         b.load_frames(b.pack_frames(frames))
         b.run()
         b.synchronize()
