@@ -112,9 +112,15 @@ def max_over_ranks(torch, world, v):
         return v
     import torch.distributed as dist
 
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    t = torch.tensor([v], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def aggregate_value(world, px_per_rank_step, max_ms_per_step):
+    """Whole-job throughput of `world` replicas: all ranks' output pixels per step
+    over the slowest rank's step time, in Mpx/s."""
+    return world * px_per_rank_step / (max_ms_per_step * 1e-3) / 1e6
 
 
 class ClockSampler:
@@ -292,7 +298,7 @@ def measure(args, torch, world, eng, d_frames, flows, stream, flush):
     ms, launches, clocks, _ = timed(False)
     ms_prof, _, _, kstats = timed(True)
     u, v = d_u.cpu().numpy(), d_v.cpu().numpy()
-    return {"ms_per_step": ms, "value": world * npairs * W * H / (ms * 1e-3) / 1e6, "launches": launches,
+    return {"ms_per_step": ms, "value": aggregate_value(world, npairs * W * H, ms), "launches": launches,
             "kstats": kstats, "ms_per_step_profiled": ms_prof, "clocks": clocks, "epe": mean_epe(u, v, flows),
             "u": u, "v": v}
 
