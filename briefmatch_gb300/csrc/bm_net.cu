@@ -1,9 +1,13 @@
 // bm_net.cu -- the learned flow proposal: a 6-layer 3x3 convolutional network at
 // quarter resolution that predicts an initial flow and a confidence for PatchMatch.
 //
-//   layer 0: 2 -> 32 channels, ReLU       (input: the two frames, quarter resolution)
-//   layers 1-4: 32 -> 32 channels, ReLU
+//   layer 0: 32 -> 32 channels, ReLU      (input: both frames at quarter resolution,
+//                                          each 4x4 block of pixels as 16 channels)
+//   layers 1-4: 32 -> 32 channels, ReLU   (dilations 2, 4, 8, 1)
 //   layer 5: 32 -> 3 channels, linear     (u/4, v/4 in quarter-resolution pixels, confidence logit)
+//
+// Every layer is a 3x3 convolution; the dilated middle layers widen the receptive
+// field to 63 cells (252 pixels) at the same cost per layer.
 //
 // Weights and activations are BF16, accumulation FP32, on the tensor cores through
 // mma.sync m16n8k16 implicit-GEMM kernels: forward, backward-data (the forward kernel
@@ -22,14 +26,26 @@
 
 namespace {
 
-constexpr int NL = 6;                              // layers
-constexpr int CIN_R[NL] = {2, 32, 32, 32, 32, 32};  // real input channels
+constexpr int NL = 6;                               // layers
+constexpr int CIN_R[NL] = {32, 32, 32, 32, 32, 32};  // real input channels
 constexpr int COUT_R[NL] = {32, 32, 32, 32, 32, 3};
-constexpr int CIN_P[NL] = {16, 32, 32, 32, 32, 32};  // padded (multiple of 16)
+constexpr int CIN_P[NL] = {32, 32, 32, 32, 32, 32};  // padded (multiple of 16)
 constexpr int COUT_P[NL] = {32, 32, 32, 32, 32, 8};  // padded (multiple of 8)
+constexpr int DIL[NL] = {1, 2, 4, 8, 1, 1};          // dilation of each layer's 3x3 taps
+constexpr int NIN = 32;                              // input channels: 16 pixels of each frame's 4x4 block
 
 constexpr int BW = 16, BH = 8;  // output tile per block: 8 rows x 16 columns, 4 warps
-constexpr int HW = BW + 2, HH = BH + 2;
+
+// Shared memory of the forward/backward-data tile (input tile with a DIL-wide halo
+// plus all nine taps' weights) and of the weight-gradient tile.
+constexpr size_t conv_smem(int cinp, int coutp, int dil)
+{
+    return ((size_t)(BH + 2 * dil) * (BW + 2 * dil) * (cinp + 8) + (size_t)9 * coutp * (cinp + 8)) * 2;
+}
+constexpr size_t wgrad_smem(int cinp, int coutd, int dil)
+{
+    return ((size_t)coutd * (BW * BH + 8) + (size_t)cinp * ((BH + 2 * dil) * (BW + 2 * dil) + 8)) * 2;
+}
 
 __device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1)
 {
@@ -48,27 +64,30 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
 
 enum Epi { EPI_RELU_BF16 = 0, EPI_LINEAR_F32 = 1, EPI_MASK_BF16 = 2 };
 
-// Y[p, co] = sum_{tap, ci} X[p + tap - 1, ci] * W[tap][co][ci]  (+ bias, ReLU) -- or,
-// for the backward-data pass, the same product followed by the ReLU mask of `act`.
-// X: [B][h][w][CINP] bf16; W: [9][COUTP][CINP] bf16; out per EPI.
-template <int CINP, int COUTP, int EPI>
+// Y[p, co] = sum_{tap, ci} X[p + DIL * (tap - 1), ci] * W[tap][co][ci]  (+ bias, ReLU) --
+// or, for the backward-data pass, the same product followed by the ReLU mask of
+// `act`.  X: [B][h][w][CINP] bf16; W: [9][COUTP][CINP] bf16; out per EPI.  Dynamic
+// shared memory: conv_smem(CINP, COUTP, DIL) bytes.
+template <int CINP, int COUTP, int EPI, int DIL>
 __global__ void __launch_bounds__(128) k_conv(const __nv_bfloat16* __restrict__ X, const __nv_bfloat16* __restrict__ W,
                                               const float* __restrict__ bias, const __nv_bfloat16* __restrict__ act,
                                               void* __restrict__ out, int h, int w, int cout_real, int out_stride)
 {
     constexpr int SP = CINP + 8;  // smem pixel stride (bf16): conflict-free fragment loads
     constexpr int NT = COUTP / 8;
-    __shared__ __align__(16) __nv_bfloat16 s_in[HH * HW * SP];
-    __shared__ __align__(16) __nv_bfloat16 s_w[9 * COUTP * SP];
+    constexpr int HW = BW + 2 * DIL, HH = BH + 2 * DIL;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __nv_bfloat16* s_in = reinterpret_cast<__nv_bfloat16*>(smem_raw);
+    __nv_bfloat16* s_w = s_in + HH * HW * SP;
     const int tid = threadIdx.x;
     const int x0 = blockIdx.x * BW, y0 = blockIdx.y * BH, b = blockIdx.z;
     const __nv_bfloat16* Xb = X + (size_t)b * h * w * CINP;
-    // stage the input tile with a one-pixel zero halo, 16 bytes at a time
+    // stage the input tile with a DIL-pixel zero halo, 16 bytes at a time
     constexpr int VPP = CINP / 8;  // 16-byte vectors per pixel
     for (int k = tid; k < HH * HW * VPP; k += 128) {
         const int pix = k / VPP, v = k - pix * VPP;
         const int hy = pix / HW, hx = pix - hy * HW;
-        const int gy = y0 + hy - 1, gx = x0 + hx - 1;
+        const int gy = y0 + hy - DIL, gx = x0 + hx - DIL;
         uint4 val = make_uint4(0, 0, 0, 0);
         if (gy >= 0 && gy < h && gx >= 0 && gx < w)
             val = *reinterpret_cast<const uint4*>(Xb + ((size_t)gy * w + gx) * CINP + v * 8);
@@ -106,8 +125,8 @@ __global__ void __launch_bounds__(128) k_conv(const __nv_bfloat16* __restrict__ 
 #pragma unroll
             for (int mt = 0; mt < 2; mt++) {
                 const int r = warp * 2 + mt;  // output row within the tile
-                const int p0 = ((r + dy) * HW + g + dx) * SP + kc * 16 + 2 * t;
-                const int p8 = ((r + dy) * HW + g + 8 + dx) * SP + kc * 16 + 2 * t;
+                const int p0 = ((r + dy * DIL) * HW + g + dx * DIL) * SP + kc * 16 + 2 * t;
+                const int p8 = ((r + dy * DIL) * HW + g + 8 + dx * DIL) * SP + kc * 16 + 2 * t;
                 uint32_t a[4];
                 a[0] = si[p0 >> 1];
                 a[1] = si[p8 >> 1];
@@ -151,22 +170,25 @@ __global__ void __launch_bounds__(128) k_conv(const __nv_bfloat16* __restrict__ 
     }
 }
 
-// dW[co][tap][ci] += sum_p dY[p, co] * X[p + tap - 1, ci] and db[co] += sum_p dY[p, co]
-// over one 8x16 tile: A = dY^T (16 output channels x 16 pixels of one tile row),
-// B = the shifted input (16 pixels x 8 input channels).  Each warp owns taps
+// dW[co][tap][ci] += sum_p dY[p, co] * X[p + DIL * (tap - 1), ci] and db[co] += sum_p
+// dY[p, co] over one 8x16 tile: A = dY^T (16 output channels x 16 pixels of one tile
+// row), B = the shifted input (16 pixels x 8 input channels).  Each warp owns taps
 // w, w+4, w+8.  Partial sums of the tile are added to the FP32 gradients atomically.
-template <int CINP, int COUTD>
+// Dynamic shared memory: wgrad_smem(CINP, COUTD, DIL) bytes.
+template <int CINP, int COUTD, int DIL>
 __global__ void __launch_bounds__(128) k_conv_wgrad(const __nv_bfloat16* __restrict__ X,
                                                     const __nv_bfloat16* __restrict__ dY, int dy_stride, int h, int w,
                                                     float* __restrict__ dW, float* __restrict__ db, int cin_real,
                                                     int cout_real)
 {
+    constexpr int HW = BW + 2 * DIL, HH = BH + 2 * DIL;
     constexpr int PX = BW * BH;        // 128 pixels
     constexpr int SPD = PX + 8;        // dY^T row stride (bf16)
     constexpr int SPX = HH * HW + 8;   // X^T row stride (bf16)
     constexpr int MT = COUTD / 16, NT = CINP / 8;
-    __shared__ __align__(16) __nv_bfloat16 s_dy[COUTD * SPD];
-    __shared__ __align__(16) __nv_bfloat16 s_x[CINP * SPX];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __nv_bfloat16* s_dy = reinterpret_cast<__nv_bfloat16*>(smem_raw);
+    __nv_bfloat16* s_x = s_dy + COUTD * SPD;
     const int tid = threadIdx.x;
     const int x0 = blockIdx.x * BW, y0 = blockIdx.y * BH, b = blockIdx.z;
     for (int k = tid; k < COUTD * PX; k += 128) {
@@ -178,7 +200,7 @@ __global__ void __launch_bounds__(128) k_conv_wgrad(const __nv_bfloat16* __restr
     }
     for (int k = tid; k < CINP * HH * HW; k += 128) {
         const int ci = k / (HH * HW), p = k - ci * (HH * HW);
-        const int gy = y0 + p / HW - 1, gx = x0 + (p % HW) - 1;
+        const int gy = y0 + p / HW - DIL, gx = x0 + (p % HW) - DIL;
         __nv_bfloat16 v = __float2bfloat16(0.0f);
         if (gy >= 0 && gy < h && gx >= 0 && gx < w) v = X[(((size_t)b * h + gy) * w + gx) * CINP + ci];
         s_x[ci * SPX + p] = v;
@@ -217,7 +239,7 @@ __global__ void __launch_bounds__(128) k_conv_wgrad(const __nv_bfloat16* __restr
 #pragma unroll
             for (int nt = 0; nt < NT; nt++) {
                 const int ci = nt * 8 + g;
-                const int row = (ks + dyy) * HW + dxx;  // shifted input row for pixels 0..15
+                const int row = (ks + dyy * DIL) * HW + dxx * DIL;  // shifted input row for pixels 0..15
                 const int base = ci * SPX + row + 2 * t;
                 const uint32_t b0 = (uint32_t)sx16[base] | ((uint32_t)sx16[base + 1] << 16);
                 const uint32_t b1 = (uint32_t)sx16[base + 8] | ((uint32_t)sx16[base + 9] << 16);
@@ -240,26 +262,33 @@ __global__ void __launch_bounds__(128) k_conv_wgrad(const __nv_bfloat16* __restr
     }
 }
 
-// Two frames -> network input: 4x4 box average of each frame, scaled to [-1, 1],
-// channels 0 and 1 of a 16-channel NHWC bf16 image (the rest zero).
+// Two frames -> network input: each frame's 4x4 pixel block of a quarter-resolution
+// cell as 16 channels (channel 4*j + i = pixel (i, j) of the block; frame 1 in
+// channels 16..31), scaled to [-1, 1], as a 32-channel NHWC bf16 image.
 __global__ void k_net_input(const uint8_t* __restrict__ f0, const uint8_t* __restrict__ f1, int W, int H,
                             __nv_bfloat16* __restrict__ out, int w4, int h4)
 {
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= w4 || y >= h4) return;
-    float s0 = 0, s1 = 0;
-    int n = 0;
-    for (int j = 0; j < 4; j++)
-        for (int i = 0; i < 4; i++) {
-            const int xx = min(W - 1, x * 4 + i), yy = min(H - 1, y * 4 + j);
-            s0 += f0[(size_t)yy * W + xx];
-            s1 += f1[(size_t)yy * W + xx];
-            n++;
+    uint32_t v[16];
+#pragma unroll
+    for (int f = 0; f < 2; f++) {
+        const uint8_t* src = f ? f1 : f0;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const int yy = min(H - 1, y * 4 + j);
+#pragma unroll
+            for (int i = 0; i < 4; i += 2) {
+                const int xa = min(W - 1, x * 4 + i), xb = min(W - 1, x * 4 + i + 1);
+                const float a = src[(size_t)yy * W + xa] / 127.5f - 1.0f;
+                const float b = src[(size_t)yy * W + xb] / 127.5f - 1.0f;
+                v[f * 8 + j * 2 + i / 2] = pack_bf16(a, b);
+            }
         }
-    uint4* o = reinterpret_cast<uint4*>(out + ((size_t)y * w4 + x) * 16);
-    const float a = s0 / n / 127.5f - 1.0f, c = s1 / n / 127.5f - 1.0f;
-    o[0] = make_uint4(pack_bf16(a, c), 0, 0, 0);
-    o[1] = make_uint4(0, 0, 0, 0);
+    }
+    uint4* o = reinterpret_cast<uint4*>(out + ((size_t)y * w4 + x) * NIN);
+#pragma unroll
+    for (int q = 0; q < 4; q++) o[q] = make_uint4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
 }
 
 // Loss of the head against BriefMatch's flow: smooth-L1 on (u, v) in quarter
@@ -349,22 +378,82 @@ __global__ void k_pack_layer(const float* __restrict__ master, int cin, int cout
     }
 }
 
-template <int CINP, int COUTP, int EPI>
+template <int CINP, int COUTP, int EPI, int D>
 cudaError_t launch_conv(const __nv_bfloat16* X, const __nv_bfloat16* W, const float* bias, const __nv_bfloat16* act,
                         void* out, int B, int h, int w, int cout_real, int out_stride, cudaStream_t st)
 {
     dim3 g((w + BW - 1) / BW, (h + BH - 1) / BH, B);
-    k_conv<CINP, COUTP, EPI><<<g, 128, 0, st>>>(X, W, bias, act, out, h, w, cout_real, out_stride);
+    k_conv<CINP, COUTP, EPI, D><<<g, 128, conv_smem(CINP, COUTP, D), st>>>(X, W, bias, act, out, h, w, cout_real,
+                                                                            out_stride);
     return cudaGetLastError();
 }
 
-template <int CINP, int COUTD>
+template <int CINP, int COUTD, int D>
 cudaError_t launch_wgrad(const __nv_bfloat16* X, const __nv_bfloat16* dY, int dy_stride, int B, int h, int w,
                          float* dW, float* db, int cin_real, int cout_real, cudaStream_t st)
 {
     dim3 g((w + BW - 1) / BW, (h + BH - 1) / BH, B);
-    k_conv_wgrad<CINP, COUTD><<<g, 128, 0, st>>>(X, dY, dy_stride, h, w, dW, db, cin_real, cout_real);
+    k_conv_wgrad<CINP, COUTD, D><<<g, 128, wgrad_smem(CINP, COUTD, D), st>>>(X, dY, dy_stride, h, w, dW, db, cin_real,
+                                                                              cout_real);
     return cudaGetLastError();
+}
+
+// Forward and backward-data of layer l (dilation DIL[l]), weight gradient of layer l.
+cudaError_t conv_fwd(int l, const __nv_bfloat16* X, const __nv_bfloat16* W, const float* bias, void* out, int B, int h,
+                     int w, cudaStream_t st)
+{
+    switch (DIL[l]) {
+    case 1: return launch_conv<32, 32, EPI_RELU_BF16, 1>(X, W, bias, nullptr, out, B, h, w, 32, 32, st);
+    case 2: return launch_conv<32, 32, EPI_RELU_BF16, 2>(X, W, bias, nullptr, out, B, h, w, 32, 32, st);
+    case 4: return launch_conv<32, 32, EPI_RELU_BF16, 4>(X, W, bias, nullptr, out, B, h, w, 32, 32, st);
+    default: return launch_conv<32, 32, EPI_RELU_BF16, 8>(X, W, bias, nullptr, out, B, h, w, 32, 32, st);
+    }
+}
+cudaError_t conv_bwd_data(int l, const __nv_bfloat16* dY, const __nv_bfloat16* Wb, const __nv_bfloat16* act, void* out,
+                          int B, int h, int w, cudaStream_t st)
+{
+    switch (DIL[l]) {
+    case 1: return launch_conv<32, 32, EPI_MASK_BF16, 1>(dY, Wb, nullptr, act, out, B, h, w, 32, 32, st);
+    case 2: return launch_conv<32, 32, EPI_MASK_BF16, 2>(dY, Wb, nullptr, act, out, B, h, w, 32, 32, st);
+    case 4: return launch_conv<32, 32, EPI_MASK_BF16, 4>(dY, Wb, nullptr, act, out, B, h, w, 32, 32, st);
+    default: return launch_conv<32, 32, EPI_MASK_BF16, 8>(dY, Wb, nullptr, act, out, B, h, w, 32, 32, st);
+    }
+}
+cudaError_t conv_wgrad(int l, const __nv_bfloat16* X, const __nv_bfloat16* dY, int B, int h, int w, float* dW, float* db,
+                       cudaStream_t st)
+{
+    switch (DIL[l]) {
+    case 1: return launch_wgrad<32, 32, 1>(X, dY, 32, B, h, w, dW, db, 32, 32, st);
+    case 2: return launch_wgrad<32, 32, 2>(X, dY, 32, B, h, w, dW, db, 32, 32, st);
+    case 4: return launch_wgrad<32, 32, 4>(X, dY, 32, B, h, w, dW, db, 32, 32, st);
+    default: return launch_wgrad<32, 32, 8>(X, dY, 32, B, h, w, dW, db, 32, 32, st);
+    }
+}
+
+// Dynamic shared-memory opt-in of every instantiation above 48 KB (once per process
+// and device; called from bm_net_create, outside any stream capture).
+cudaError_t conv_smem_optin()
+{
+    static bool done[64] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 64 && done[dev]) return cudaSuccess;
+    auto set = [](const void* f, size_t bytes) {
+        return cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    };
+    const cudaError_t es[] = {
+        set((const void*)k_conv<32, 32, EPI_RELU_BF16, 4>, conv_smem(32, 32, 4)),
+        set((const void*)k_conv<32, 32, EPI_RELU_BF16, 8>, conv_smem(32, 32, 8)),
+        set((const void*)k_conv<32, 32, EPI_MASK_BF16, 4>, conv_smem(32, 32, 4)),
+        set((const void*)k_conv<32, 32, EPI_MASK_BF16, 8>, conv_smem(32, 32, 8)),
+        set((const void*)k_conv_wgrad<32, 32, 4>, wgrad_smem(32, 32, 4)),
+        set((const void*)k_conv_wgrad<32, 32, 8>, wgrad_smem(32, 32, 8)),
+    };
+    for (cudaError_t x : es)
+        if (x != cudaSuccess) return x;
+    if (dev < 64) done[dev] = true;
+    return cudaSuccess;
 }
 
 size_t layer_w_count(int l) { return (size_t)COUT_R[l] * 9 * CIN_R[l]; }
@@ -382,7 +471,7 @@ struct bm_net {
     float* d_v = nullptr;
     __nv_bfloat16* d_wf[NL] = {};
     __nv_bfloat16* d_wb[NL] = {};
-    __nv_bfloat16* d_in = nullptr;      // [B][h][w][16]
+    __nv_bfloat16* d_in = nullptr;      // [B][h][w][32]
     __nv_bfloat16* d_act[NL - 1] = {};  // outputs of layers 0..4, [B][h][w][32]
     __nv_bfloat16* d_dy[2] = {};        // gradient ping-pong, [B][h][w][32]
     float* d_out = nullptr;             // [B][h][w][3]
@@ -436,14 +525,11 @@ bm_status forward(bm_net* n, uint32_t B, uint32_t h, uint32_t w, cudaStream_t st
         if (s != BM_OK) return s;
     }
     const int Bi = (int)B, hi = (int)h, wi = (int)w;
-    BN_CUDA((launch_conv<16, 32, EPI_RELU_BF16>(n->d_in, n->d_wf[0], n->d_master + n->poff[0] + layer_w_count(0),
-                                                nullptr, n->d_act[0], Bi, hi, wi, 32, 32, st)));
-    for (int l = 1; l <= 4; l++)
-        BN_CUDA((launch_conv<32, 32, EPI_RELU_BF16>(n->d_act[l - 1], n->d_wf[l],
-                                                    n->d_master + n->poff[l] + layer_w_count(l), nullptr, n->d_act[l],
-                                                    Bi, hi, wi, 32, 32, st)));
-    BN_CUDA((launch_conv<32, 8, EPI_LINEAR_F32>(n->d_act[4], n->d_wf[5], n->d_master + n->poff[5] + layer_w_count(5),
-                                                nullptr, n->d_out, Bi, hi, wi, 3, 3, st)));
+    for (int l = 0; l <= 4; l++)
+        BN_CUDA(conv_fwd(l, l == 0 ? n->d_in : n->d_act[l - 1], n->d_wf[l], n->d_master + n->poff[l] + layer_w_count(l),
+                         n->d_act[l], Bi, hi, wi, st));
+    BN_CUDA((launch_conv<32, 8, EPI_LINEAR_F32, 1>(n->d_act[4], n->d_wf[5], n->d_master + n->poff[5] + layer_w_count(5),
+                                                   nullptr, n->d_out, Bi, hi, wi, 3, 3, st)));
     return BM_OK;
 }
 
@@ -461,6 +547,7 @@ size_t bm_net_param_count(void)
 bm_status bm_net_create(uint32_t max_batch, uint32_t max_h4, uint32_t max_w4, bm_net** out)
 {
     if (!out || max_batch == 0 || max_h4 == 0 || max_w4 == 0) return nfail(BM_ERR_INVALID, "bm_net_create: bad size");
+    if (conv_smem_optin() != cudaSuccess) return nfail(BM_ERR_CUDA, "bm_net_create: shared-memory opt-in failed");
     bm_net* n = new bm_net();
     n->maxB = max_batch;
     n->maxh = max_h4;
@@ -475,7 +562,7 @@ bm_status bm_net_create(uint32_t max_batch, uint32_t max_h4, uint32_t max_w4, bm
     bool ok = cudaMalloc((void**)&n->d_master, off * 4) == cudaSuccess &&
               cudaMalloc((void**)&n->d_grad, off * 4) == cudaSuccess &&
               cudaMalloc((void**)&n->d_m, off * 4) == cudaSuccess && cudaMalloc((void**)&n->d_v, off * 4) == cudaSuccess &&
-              cudaMalloc((void**)&n->d_in, px * 16 * 2) == cudaSuccess &&
+              cudaMalloc((void**)&n->d_in, px * NIN * 2) == cudaSuccess &&
               cudaMalloc((void**)&n->d_out, px * 3 * 4) == cudaSuccess &&
               cudaMalloc((void**)&n->d_loss, 4 * 4) == cudaSuccess &&
               cudaMalloc((void**)&n->d_dy[0], px * 32 * 2) == cudaSuccess &&
@@ -559,19 +646,19 @@ bm_status bm_net_prepare(bm_net* n, uint32_t b, const uint8_t* d_f0, const uint8
     if (b >= n->maxB || (size_t)w4 * h4 > (size_t)n->maxh * n->maxw || w4 == 0 || h4 == 0)
         return nfail(BM_ERR_LIMIT, "bm_net_prepare: beyond the network's buffers");
     dim3 blk(32, 8), g((w4 + 31) / 32, (h4 + 7) / 8);
-    k_net_input<<<g, blk, 0, (cudaStream_t)stream>>>(d_f0, d_f1, (int)W, (int)H, n->d_in + (size_t)b * h4 * w4 * 16,
+    k_net_input<<<g, blk, 0, (cudaStream_t)stream>>>(d_f0, d_f1, (int)W, (int)H, n->d_in + (size_t)b * h4 * w4 * NIN,
                                                      (int)w4, (int)h4);
     BN_CUDA(cudaGetLastError());
     return BM_OK;
 }
 
-// Raw network input (bf16 NHWC, 16 channels) for tests.
+// Raw network input (bf16 NHWC, 32 channels) for tests.
 bm_status bm_net_set_input(bm_net* n, const uint16_t* d_in, uint32_t B, uint32_t h, uint32_t w, void* stream)
 {
     if (!n || !d_in) return nfail(BM_ERR_INVALID, "bm_net_set_input: null");
     bm_status s = check_dims(n, B, h, w);
     if (s != BM_OK) return s;
-    BN_CUDA(cudaMemcpyAsync(n->d_in, d_in, (size_t)B * h * w * 16 * 2, cudaMemcpyDeviceToDevice, (cudaStream_t)stream));
+    BN_CUDA(cudaMemcpyAsync(n->d_in, d_in, (size_t)B * h * w * NIN * 2, cudaMemcpyDeviceToDevice, (cudaStream_t)stream));
     return BM_OK;
 }
 
@@ -609,20 +696,18 @@ bm_status bm_net_train_step(bm_net* n, uint32_t B, uint32_t h, uint32_t w, const
     BN_CUDA(cudaGetLastError());
     // layer 5: dY (16 padded channels, 3 real) -> dW5, and dX into the ReLU mask of act[4]
     float* g = n->d_grad;
-    BN_CUDA((launch_wgrad<32, 16>(n->d_act[4], n->d_dy[0], 16, Bi, hi, wi, g + n->poff[5], g + n->poff[5] + layer_w_count(5),
-                                  32, 3, st)));
-    BN_CUDA((launch_conv<16, 32, EPI_MASK_BF16>(n->d_dy[0], n->d_wb[5], nullptr, n->d_act[4], n->d_dy[1], Bi, hi, wi, 32,
-                                                32, st)));
+    BN_CUDA((launch_wgrad<32, 16, 1>(n->d_act[4], n->d_dy[0], 16, Bi, hi, wi, g + n->poff[5],
+                                     g + n->poff[5] + layer_w_count(5), 32, 3, st)));
+    BN_CUDA((launch_conv<16, 32, EPI_MASK_BF16, 1>(n->d_dy[0], n->d_wb[5], nullptr, n->d_act[4], n->d_dy[1], Bi, hi, wi,
+                                                   32, 32, st)));
     int cur = 1;
     for (int l = 4; l >= 1; l--) {
-        BN_CUDA((launch_wgrad<32, 32>(n->d_act[l - 1], n->d_dy[cur], 32, Bi, hi, wi, g + n->poff[l],
-                                      g + n->poff[l] + layer_w_count(l), 32, 32, st)));
-        BN_CUDA((launch_conv<32, 32, EPI_MASK_BF16>(n->d_dy[cur], n->d_wb[l], nullptr, n->d_act[l - 1], n->d_dy[cur ^ 1],
-                                                    Bi, hi, wi, 32, 32, st)));
+        BN_CUDA(conv_wgrad(l, n->d_act[l - 1], n->d_dy[cur], Bi, hi, wi, g + n->poff[l], g + n->poff[l] + layer_w_count(l),
+                           st));
+        BN_CUDA(conv_bwd_data(l, n->d_dy[cur], n->d_wb[l], n->d_act[l - 1], n->d_dy[cur ^ 1], Bi, hi, wi, st));
         cur ^= 1;
     }
-    BN_CUDA((launch_wgrad<16, 32>(n->d_in, n->d_dy[cur], 32, Bi, hi, wi, g + n->poff[0], g + n->poff[0] + layer_w_count(0),
-                                  2, 32, st)));
+    BN_CUDA(conv_wgrad(0, n->d_in, n->d_dy[cur], Bi, hi, wi, g + n->poff[0], g + n->poff[0] + layer_w_count(0), st));
     if (d_grad_out) BN_CUDA(cudaMemcpyAsync(d_grad_out, g, n->nparam * 4, cudaMemcpyDeviceToDevice, st));
     if (lr > 0) {
         n->step++;

@@ -42,8 +42,9 @@ def _declare():
 
 def flops_per_pixel():
     """Multiply-add FLOPs of one forward pass per quarter-resolution pixel (real
-    channels: 3x3 taps, 2 -> 32, four 32 -> 32, 32 -> 3)."""
-    cin = [2, 32, 32, 32, 32, 32]
+    channels: 3x3 taps, five 32 -> 32 (the first on both frames' 4x4 pixel blocks),
+    32 -> 3)."""
+    cin = [32, 32, 32, 32, 32, 32]
     cout = [32, 32, 32, 32, 32, 3]
     return sum(2 * 9 * a * b for a, b in zip(cin, cout))
 

@@ -263,20 +263,22 @@ bm_status bm_selftest_barrier(uint32_t blocks, uint32_t expect, uint64_t spin_li
 
 /* ---- learned flow proposal ---------------------------------------------------------- */
 
-/* No counterpart in the reference.  A 6-layer 3x3 convolutional network (2->32, 4x
- * 32->32, 32->3; ReLU between) on the two frames at quarter resolution, BF16 weights
- * and activations with FP32 accumulation on the tensor cores, predicting the flow
- * (quarter-resolution pixels) and a confidence logit per quarter-resolution pixel.
- * Parameters are one FP32 vector: for each layer W[cout][9][cin] then b[cout]. */
+/* No counterpart in the reference.  A 6-layer 3x3 convolutional network (32->32 x5,
+ * 32->3; ReLU between; dilations 1, 2, 4, 8, 1, 1) on the two frames at quarter
+ * resolution -- each frame's 4x4 pixel block of a cell as 16 input channels -- with
+ * BF16 weights and activations and FP32 accumulation on the tensor cores, predicting
+ * the flow (quarter-resolution pixels) and a confidence logit per cell.  Parameters
+ * are one FP32 vector: for each layer W[cout][9][cin] then b[cout]. */
 size_t bm_net_param_count(void);
 bm_status bm_net_create(uint32_t max_batch, uint32_t max_h4, uint32_t max_w4, bm_net** out);
 bm_status bm_net_destroy(bm_net* n);
 bm_status bm_net_set_params(bm_net* n, const float* h_params, size_t count);
 bm_status bm_net_get_params(bm_net* n, float* h_params, size_t count);
-/* Input image b from two 8-bit W x H device frames (4x4 box average, [-1, 1]). */
+/* Input image b from two 8-bit W x H device frames (channel 4*j + i of cell (x, y):
+ * pixel (4x + i, 4y + j) of frame 0 scaled to [-1, 1]; channels 16..31: frame 1). */
 bm_status bm_net_prepare(bm_net* n, uint32_t b, const uint8_t* d_f0, const uint8_t* d_f1, uint32_t W, uint32_t H,
                          void* stream);
-/* Raw input: B images h x w, bf16 NHWC with 16 channels (channels 0,1 used). */
+/* Raw input: B images h x w, bf16 NHWC with 32 channels. */
 bm_status bm_net_set_input(bm_net* n, const uint16_t* d_in, uint32_t B, uint32_t h, uint32_t w, void* stream);
 /* Forward; d_out (may be NULL) receives [B][h][w][3] floats (u, v, confidence logit). */
 bm_status bm_net_forward(bm_net* n, uint32_t B, uint32_t h, uint32_t w, float* d_out, void* stream);

@@ -9,8 +9,9 @@ from __future__ import annotations
 
 import numpy as np
 
-CIN = [2, 32, 32, 32, 32, 32]
+CIN = [32, 32, 32, 32, 32, 32]
 COUT = [32, 32, 32, 32, 32, 3]
+DIL = [1, 2, 4, 8, 1, 1]   # dilation of each layer's 3x3 taps
 
 
 def bf16(x):
@@ -32,16 +33,17 @@ def unpack(params):
     return out
 
 
-def _shifts(x):
-    """The 9 zero-padded 3x3 neighbours of NHWC x: list of [B,h,w,C] (tap = dy*3+dx)."""
+def _shifts(x, d=1):
+    """The 9 zero-padded 3x3 neighbours at dilation d of NHWC x: list of [B,h,w,C]
+    (tap = dy*3+dx, offset d*(dy-1, dx-1))."""
     B, h, w, C = x.shape
-    p = np.zeros((B, h + 2, w + 2, C), np.float32)
-    p[:, 1:-1, 1:-1] = x
-    return [p[:, dy:dy + h, dx:dx + w] for dy in range(3) for dx in range(3)]
+    p = np.zeros((B, h + 2 * d, w + 2 * d, C), np.float32)
+    p[:, d:d + h, d:d + w] = x
+    return [p[:, dy * d:dy * d + h, dx * d:dx * d + w] for dy in range(3) for dx in range(3)]
 
 
-def conv(x, W, b=None):
-    sh = _shifts(x)
+def conv(x, W, b=None, d=1):
+    sh = _shifts(x, d)
     y = sum(np.einsum("bhwc,oc->bhwo", sh[t], W[:, t, :], optimize=True) for t in range(9))
     return y + (b if b is not None else 0)
 
@@ -56,10 +58,10 @@ def forward(params, x0, rounding=True):
     x = _r(x0, rounding)
     for l in range(5):
         W, b = layers[l]
-        x = _r(np.maximum(conv(x, _r(W, rounding), b), 0), rounding)
+        x = _r(np.maximum(conv(x, _r(W, rounding), b, DIL[l]), 0), rounding)
         acts.append(x)
     W, b = layers[5]
-    return conv(x, _r(W, rounding), b).astype(np.float32), acts
+    return conv(x, _r(W, rounding), b, DIL[5]).astype(np.float32), acts
 
 
 def loss_grad(out, target, tau=1.0, wconf=0.25, rounding=True):
@@ -93,14 +95,14 @@ def backward(params, x0, acts, dY, rounding=True):
     for l in range(5, -1, -1):
         W, _ = layers[l]
         X = xs[l]
-        sh = _shifts(X)
+        sh = _shifts(X, DIL[l])
         dW = np.stack([np.einsum("bhwo,bhwc->oc", dY, sh[t], optimize=True) for t in range(9)], axis=1)
         db = dY.sum(axis=(0, 1, 2))
         grads.append((dW, db))
         if l > 0:
             # dX[q] = sum_t dY[q - off(t)] W[:, t, :]: correlation with the flipped kernel
             Wf = _r(W, rounding)[:, ::-1, :]
-            shd = _shifts(dY)
+            shd = _shifts(dY, DIL[l])
             dX = sum(np.einsum("bhwo,oc->bhwc", shd[t], Wf[:, t, :], optimize=True) for t in range(9))
             dY = _r(dX * (acts[l - 1] > 0), rounding)
     grads = grads[::-1]

@@ -27,19 +27,57 @@ def _setup(B=2, h=20, w=36, seed=0):
     p = net.params()
     p += rng.normal(0, 0.02, p.size).astype(np.float32)  # non-zero biases too
     net.set_params(p)
-    x = np.zeros((B, h, w, 16), np.float32)
-    x[..., :2] = rng.uniform(-1, 1, (B, h, w, 2))
+    x = rng.uniform(-1, 1, (B, h, w, net_oracle.CIN[0])).astype(np.float32)
     d_in = torch.from_numpy(_bf16_bits(x).view(np.int16)).cuda()
     net.set_input(d_in.data_ptr(), B, h, w)
     tgt = np.zeros((B, h, w, 3), np.float32)
     tgt[..., 0] = rng.normal(0, 1.5, (B, h, w))
     tgt[..., 1] = rng.normal(0, 1.5, (B, h, w))
     tgt[..., 2] = (rng.uniform(size=(B, h, w)) > 0.1).astype(np.float32)
-    return net, p, x[..., :2], tgt
+    return net, p, x, tgt
 
 
 def test_param_count():
-    assert param_count() == 2 * 9 * 32 + 32 + 4 * (32 * 9 * 32 + 32) + 3 * 9 * 32 + 3
+    assert param_count() == 5 * (32 * 9 * 32 + 32) + 3 * 9 * 32 + 3
+
+
+def test_input_preparation():
+    """bm_net_prepare: channel 4*j + i of cell (x, y) is pixel (4x + i, 4y + j) of frame 0
+    scaled to [-1, 1] (BF16), channels 16..31 the same for frame 1."""
+    W, H = 40, 24
+    rng = np.random.default_rng(9)
+    f0 = rng.integers(0, 256, (H, W), dtype=np.uint8)
+    f1 = rng.integers(0, 256, (H, W), dtype=np.uint8)
+    h4, w4 = H // 4, W // 4
+    net = ProposalNet(1, h4, w4)
+    p = net.params()
+    p[:] = 0
+    # layers 0-4: identity on all 32 channels through the centre tap (ReLU keeps the
+    # non-negative inputs); the head reads frame-0 pixel (0, 0) as u and frame-1
+    # pixel (3, 3) as v
+    d0, d1 = torch.from_numpy(f0).cuda(), torch.from_numpy(f1).cuda()
+    net.prepare(0, d0.data_ptr(), d1.data_ptr(), W, H)
+    k = 0
+    dims = list(zip(net_oracle.CIN, net_oracle.COUT))
+    for l, (ci, co) in enumerate(dims):
+        Wl = np.zeros((co, 9, ci), np.float32)
+        if l < 5:
+            for c in range(min(ci, co)):
+                Wl[c, 4, c] = 1.0
+        else:
+            Wl[0, 4, 0] = 1.0
+            Wl[1, 4, 16 + 15] = 1.0
+        p[k:k + co * 9 * ci] = Wl.ravel()
+        k += co * 9 * ci + co
+    net.set_params(p)
+    out = torch.empty(1, h4, w4, 3, device="cuda")
+    net.forward(1, h4, w4, out.data_ptr())
+    torch.cuda.synchronize()
+    o = out[0].cpu().numpy()
+    bf = lambda a: net_oracle.bf16(a.astype(np.float32) / np.float32(127.5) - np.float32(1.0))
+    want_u = np.maximum(bf(f0[0::4, 0::4]), 0)
+    want_v = np.maximum(bf(f1[3::4, 3::4]), 0)
+    assert np.array_equal(o[..., 0], want_u) and np.array_equal(o[..., 1], want_v)
 
 
 def test_forward_matches_oracle():

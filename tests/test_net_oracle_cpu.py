@@ -18,10 +18,11 @@ def test_gradient_matches_finite_differences():
     rng = np.random.default_rng(0)
     n = sum(co * 9 * ci + co for ci, co in zip(net_oracle.CIN, net_oracle.COUT))
     p = rng.normal(0, 0.15, n).astype(np.float64).astype(np.float32)
-    x = rng.uniform(-1, 1, (1, 6, 7, 2)).astype(np.float32)
-    t = np.zeros((1, 6, 7, 3), np.float32)
-    t[..., 0] = rng.normal(0, 3, (1, 6, 7))
-    t[..., 1] = rng.normal(0, 3, (1, 6, 7))
+    shape = (1, 11, 12)  # wider than the largest dilation (8), so every tap reaches in
+    x = rng.uniform(-1, 1, shape + (net_oracle.CIN[0],)).astype(np.float32)
+    t = np.zeros(shape + (3,), np.float32)
+    t[..., 0] = rng.normal(0, 3, shape)
+    t[..., 1] = rng.normal(0, 3, shape)
     t[..., 2] = 1.0
     out, acts = net_oracle.forward(p, x, rounding=False)
     dY, _ = net_oracle.loss_grad(out, t, rounding=False)
