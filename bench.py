@@ -199,7 +199,8 @@ def make_workload(rank):
 
 
 def algorithmic_bytes(kernel, prm):
-    """Bytes one launch must move at minimum (the per-unit figures in the design doc)."""
+    """Bytes one launch must move at minimum: per unit (pixel), the data the kernel
+    must read and write once."""
     n = prm.sx * prm.sy
     ni = prm.sx_in * prm.sy_in
     ns = (prm.N + 31) // 32

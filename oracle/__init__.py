@@ -1,8 +1,8 @@
 """The oracle: CPU restatement of the BriefMatch flow path (TEST INFRASTRUCTURE).
 
 Only the tests, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg may use
-this package, and only as the checker or the timed CPU baseline, never as the
-engine.  It wraps oracle/_build/libbmoracle.so (bm_oracle.c) with numpy arrays in
+this package, and only as the reference the engine is compared with or as the
+timed CPU baseline, never as the engine.  It wraps oracle/_build/libbmoracle.so (bm_oracle.c) with numpy arrays in
 the reference's layouts: float images, uint32 descriptors [sx*sy][ceil(N/32)],
 int16 NX/NY, uint16 Hamming costs.
 """

@@ -1,8 +1,8 @@
 /*
  * bm_oracle.c -- CPU restatement of the BriefMatch flow path (TEST INFRASTRUCTURE).
  *
- * This is the checker for the GB300 engine and the CPU baseline that bench.py
- * times; it is never linked into the engine.  Each function cites the reference
+ * The tests compare the GB300 engine with it, and bench.py times it as the CPU
+ * baseline; it is never linked into the engine.  Each function cites the reference
  * file:line it restates.  Arithmetic mirrors the reference's types (float with
  * fused multiply-add where the CUDA build contracts a*b+c, int16 flow, integer
  * Hamming distance); transcendental functions come from libm, so results that

@@ -1,8 +1,9 @@
 /*
  * bm_oracle.h -- CPU restatement of the BriefMatch flow path (TEST INFRASTRUCTURE).
  *
- * This library is the checker for the GB300 engine, never part of it: only the
- * tests, the smoke check and bench.py's CPU-baseline leg may load it.  Every
+ * The tests compare the GB300 engine with this library; it is never part of the
+ * engine: only the tests, the smoke check and bench.py's CPU-baseline leg may
+ * load it.  Every
  * function restates one piece of the reference algorithm in plain C (scalar,
  * with OpenMP over rows) and cites the reference file:line it follows.
  *

@@ -1,5 +1,5 @@
 """FP32 CPU restatement of the proposal network's forward and backward passes
-(TEST INFRASTRUCTURE, the checker of the tensor-core kernels).
+(TEST INFRASTRUCTURE: the tensor-core kernels are compared with it).
 
 It rounds to BF16 exactly where the GPU stores BF16 (weights, the network input,
 every ReLU activation, every activation gradient), so that the GPU and this

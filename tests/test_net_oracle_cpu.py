@@ -1,6 +1,6 @@
 """The proposal network's CPU restatement: its analytic gradient agrees with finite
-differences of its own loss (without BF16 rounding), which pins the checker the GPU
-kernels are compared with."""
+differences of its own loss (without BF16 rounding), which pins the restatement the
+GPU kernels are compared with."""
 from __future__ import annotations
 
 import numpy as np
