@@ -78,6 +78,7 @@ def parse():
     ap.add_argument("--no-batched", action="store_true", help="skip the 64-pair batched workload")
     ap.add_argument("--batch-pairs", type=int, default=64)
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-seeded engine")
+    ap.add_argument("--no-pipelined", action="store_true", help="finish every frame before the next")
     ap.add_argument("--config", default="2", choices=sorted(CONFIGS),
                     help="workload: 1 = 584x388 u1.5 N32 pair, 2 = 1024x436 u2.9 N128 8-frame sequence (default), "
                          "3 = 1920x1080 u4.9 N512 5-frame sequence; 1 and 3 run the plain engine beside the "
@@ -224,6 +225,7 @@ def algorithmic_bytes(kernel, prm):
 
 
 PROPOSAL_CONF = 0.5
+PIPELINED = True   # each pair's refinement overlaps the next frame (bm_set_pipelined)
 SCHEDULE_CANDIDATES = ((1, 16), (1, 32), (1, 64), (1, 128), (1, 256), (2, 16), (2, 32), (2, 64))
 
 
@@ -236,16 +238,21 @@ def open_engine(torch, prm, pattern, stream, net=None, schedule=None):
     eng.set_stream(stream.cuda_stream)
     if net is not None:
         bm.set_proposal(eng, net, PROPOSAL_CONF, schedule[0], schedule[1])
+    if PIPELINED:
+        eng.set_pipelined(True)
     return eng
 
 
 def sequence_step(eng, frame_ptrs, u_ptrs, v_ptrs, on_device):
-    """One step: the whole sequence from the same random-stream position."""
+    """One step: the whole sequence from the same random-stream position.  With
+    pipelined frames the engine stream then waits for the last refinement, so work
+    queued after the step (the end event) follows all of it."""
     eng.reset_sequence()
     eng.set_rng_position(0)
     eng.frame(frame_ptrs[0], on_device)
     for k in range(1, len(frame_ptrs)):
         eng.frame(frame_ptrs[k], on_device, u_ptrs[k - 1], v_ptrs[k - 1], on_device)
+    eng.join()
 
 
 def mean_epe(u, v, flows):
@@ -491,6 +498,7 @@ def run_engine(args, torch, world, rank):
                    "frames_per_step": FRAMES, "pairs_per_step": PAIRS, "upsampling": UP, "feature_length": NBITS,
                    "grid": [prm.sx, prm.sy], "iterations": sched["iterations"], "jfMax": sched["jfMax"],
                    "fsize": prm.fsize, "l2": "flushed (256 MB write) before every timed step",
+                   "pipelined": PIPELINED,
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "epe": {"mean": float(np.mean(head["epe"])), "per_pair": [round(e, 4) for e in head["epe"]],
                 "plain_mean": float(np.mean(rp["epe"]))},
@@ -760,6 +768,8 @@ def reference_cuda(torch, prm, pattern, frames, args):
 def main():
     args = parse()
     set_config(args.config)
+    global PIPELINED
+    PIPELINED = not args.no_pipelined
     if args.config != "2":
         args.no_learned = args.no_batched = args.no_cpu_baseline = True
     import torch

@@ -104,6 +104,8 @@ def _declare(lib):
         "bm_profile_reset": (c.c_int, [c.c_void_p]),
         "bm_profile_read": (c.c_int, [c.c_void_p, c.c_void_p, c.c_uint32, P(c.c_uint32)]),
         "bm_set_proposal": (c.c_int, [c.c_void_p, c.c_void_p, c.c_float, c.c_uint32, c.c_uint32]),
+        "bm_set_pipelined": (c.c_int, [c.c_void_p, c.c_int]),
+        "bm_join": (c.c_int, [c.c_void_p]),
         "bm_batch_set_proposal": (c.c_int, [c.c_void_p, c.c_void_p, c.c_float, c.c_uint32, c.c_uint32]),
         "bm_seed": (c.c_int, [c.c_void_p, c.c_int, c.c_void_p, c.c_uint32, c.c_uint32, c.c_float]),
         "bm_refine_noalloc": (c.c_int, [c.c_void_p, c.c_void_p, c.c_void_p, c.c_void_p, c.c_void_p, c.c_uint32,
@@ -353,6 +355,14 @@ class BriefMatch:
 
     def reset_sequence(self):
         check(lib().bm_reset_sequence(self.ctx))
+
+    def set_pipelined(self, on=True):
+        """Overlap each pair's refinement with the next frame (bm_set_pipelined)."""
+        check(lib().bm_set_pipelined(self.ctx, int(bool(on))))
+
+    def join(self):
+        """The context stream waits for the pipelined refinement queued so far."""
+        check(lib().bm_join(self.ctx))
 
     def launch_count(self):
         return int(lib().bm_launch_count(self.ctx))

@@ -60,16 +60,29 @@ struct bm_ctx {
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
 
-    uint8_t* d_u8[2] = {nullptr, nullptr};   // 8-bit frames, [cur_frame] current
-    float* d_frame[2] = {nullptr, nullptr};  // [cur_frame] current, [cur_frame^1] previous
+    // frames in a ring of three: [cur_frame] receives the next frame, [prev] holds the
+    // previous one (a third slot lets a pipelined refinement keep reading its guide)
+    uint8_t* d_u8[3] = {nullptr, nullptr, nullptr};
+    float* d_frame[3] = {nullptr, nullptr, nullptr};
     int cur_frame = 0;
+    int prev_frame() const { return (cur_frame + 2) % 3; }
     float* d_up = nullptr;
     uint32_t* d_feat[2] = {nullptr, nullptr};
     int feat1 = 0;                           // d_feat[feat1] is FEAT1, d_feat[feat1^1] FEAT2
     uint32_t* d_flow[2] = {nullptr, nullptr};
     int flow_cur = 0;
     uint16_t* d_cost = nullptr;
-    float* d_flow_in = nullptr;    // U then V, npix_in each
+    float* d_flow_in = nullptr;    // U then V, npix_in each (one of d_flow_in_buf)
+    float* d_flow_in_buf[2] = {nullptr, nullptr};
+    int flow_in_slot = 0;
+    // pipelined bm_frame (bm_set_pipelined): refinement and output copies of a pair on
+    // refine_stream, overlapping the next pair's matching on the context stream
+    bool pipelined = false;
+    cudaStream_t refine_stream = nullptr;
+    cudaEvent_t ev_ready = nullptr;               // context stream: pair down-sampled
+    cudaEvent_t ev_frame_free[3] = {};            // refine stream: guide frame slot released
+    cudaEvent_t ev_flowin_free[2] = {};           // refine stream: down-sampled flow released
+    cudaEvent_t ev_refined = nullptr;             // refine stream: last refinement and copies done
     float* d_flow_med = nullptr;
     float* d_flow_out = nullptr;
     float* d_tmp = nullptr;
@@ -148,6 +161,7 @@ void prof_end(bm_ctx* c, const char* name, cudaEvent_t a, cudaEvent_t b)
 cudaError_t prof_collect(bm_ctx* c)
 {
     cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e == cudaSuccess && c->refine_stream) e = cudaStreamSynchronize(c->refine_stream);
     if (e != cudaSuccess) return e;
     for (auto& r : c->prof_pending) {
         float ms = 0;
@@ -183,8 +197,9 @@ bm_status dev_alloc(T** p, size_t count)
 
 void release(bm_ctx* c)
 {
-    void* ptrs[] = {c->d_u8[0], c->d_u8[1], c->d_pred, c->d_frame[0], c->d_frame[1], c->d_up, c->d_feat[0], c->d_feat[1],
-                    c->d_flow[0], c->d_flow[1], c->d_cost, c->d_flow_in, c->d_flow_med, c->d_flow_out,
+    void* ptrs[] = {c->d_u8[0], c->d_u8[1], c->d_u8[2], c->d_pred, c->d_frame[0], c->d_frame[1], c->d_frame[2], c->d_up,
+                    c->d_feat[0], c->d_feat[1], c->d_flow[0], c->d_flow[1], c->d_cost, c->d_flow_in_buf[0],
+                    c->d_flow_in_buf[1], c->d_flow_med, c->d_flow_out,
                     c->d_tmp, c->d_pattern, c->d_taps, c->d_lx, c->d_ix, c->d_ly, c->d_iy,
                     c->d_nnx, c->d_nny};
     for (void* p : ptrs)
@@ -194,7 +209,19 @@ void release(bm_ctx* c)
         cudaEventDestroy(r.b);
     }
     for (cudaEvent_t e : c->prof_pool) cudaEventDestroy(e);
+    cudaEvent_t evs[] = {c->ev_ready, c->ev_refined, c->ev_frame_free[0], c->ev_frame_free[1], c->ev_frame_free[2],
+                         c->ev_flowin_free[0], c->ev_flowin_free[1]};
+    for (cudaEvent_t e : evs)
+        if (e) cudaEventDestroy(e);
+    if (c->refine_stream) cudaStreamDestroy(c->refine_stream);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
+}
+
+// The context stream waits for the pipelined refinement queued so far (no-op otherwise).
+cudaError_t join_refine(bm_ctx* c)
+{
+    if (!c->refine_stream) return cudaSuccess;
+    return cudaStreamWaitEvent(c->stream, c->ev_refined, 0);
 }
 
 bm_status check_ctx(const bm_ctx* c)
@@ -416,18 +443,18 @@ bm_status bm_create(const bm_params* prm, bm_ctx** out)
     }
     c->stream = c->own_stream;
     const size_t n = c->npix, ni = c->npix_in;
-    BM_TRY(dev_alloc(&c->d_u8[0], ni));
-    BM_TRY(dev_alloc(&c->d_u8[1], ni));
+    for (int k = 0; k < 3; k++) BM_TRY(dev_alloc(&c->d_u8[k], ni));
     BM_TRY(dev_alloc(&c->d_pred, (size_t)(p.sx_in / 4 + 1) * (p.sy_in / 4 + 1) * 3));
-    BM_TRY(dev_alloc(&c->d_frame[0], ni));
-    BM_TRY(dev_alloc(&c->d_frame[1], ni));
+    for (int k = 0; k < 3; k++) BM_TRY(dev_alloc(&c->d_frame[k], ni));
     BM_TRY(dev_alloc(&c->d_up, n));
     BM_TRY(dev_alloc(&c->d_feat[0], n * c->nsp));
     BM_TRY(dev_alloc(&c->d_feat[1], n * c->nsp));
     BM_TRY(dev_alloc(&c->d_flow[0], n));
     BM_TRY(dev_alloc(&c->d_flow[1], n));
     BM_TRY(dev_alloc(&c->d_cost, n));
-    BM_TRY(dev_alloc(&c->d_flow_in, 2 * ni));
+    BM_TRY(dev_alloc(&c->d_flow_in_buf[0], 2 * ni));
+    BM_TRY(dev_alloc(&c->d_flow_in_buf[1], 2 * ni));
+    c->d_flow_in = c->d_flow_in_buf[0];
     BM_TRY(dev_alloc(&c->d_flow_med, 2 * ni));
     BM_TRY(dev_alloc(&c->d_flow_out, 2 * ni));
     BM_TRY(dev_alloc(&c->d_tmp, 2 * ni));
@@ -456,8 +483,8 @@ bm_status bm_create(const bm_params* prm, bm_ctx** out)
     if (!cu(cudaMemsetAsync(c->d_flow[1], 0, n * sizeof(uint32_t), c->stream))) return BM_ERR_CUDA;
     if (!cu(cudaMemsetAsync(c->d_cost, 0, n * sizeof(uint16_t), c->stream))) return BM_ERR_CUDA;
     if (!cu(cudaMemsetAsync(c->d_flow_out, 0, 2 * ni * sizeof(float), c->stream))) return BM_ERR_CUDA;
-    if (!cu(cudaMemsetAsync(c->d_frame[0], 0, ni * sizeof(float), c->stream))) return BM_ERR_CUDA;
-    if (!cu(cudaMemsetAsync(c->d_frame[1], 0, ni * sizeof(float), c->stream))) return BM_ERR_CUDA;
+    for (int k = 0; k < 3; k++)
+        if (!cu(cudaMemsetAsync(c->d_frame[k], 0, ni * sizeof(float), c->stream))) return BM_ERR_CUDA;
     if (!cu(cudaMemcpyAsync(c->d_taps, taps, P * sizeof(float), cudaMemcpyHostToDevice, c->stream))) return BM_ERR_CUDA;
     if (!cu(bmk::lanczos_tables(c->d_lx, c->d_ix, (int)p.sx_in, (int)p.sx, c->stream))) return BM_ERR_CUDA;
     if (!cu(bmk::lanczos_tables(c->d_ly, c->d_iy, (int)p.sy_in, (int)p.sy, c->stream))) return BM_ERR_CUDA;
@@ -480,6 +507,7 @@ bm_status bm_destroy(bm_ctx* c)
 {
     if (!c) return BM_OK;
     cudaStreamSynchronize(c->stream);
+    if (c->refine_stream) cudaStreamSynchronize(c->refine_stream);
     release(c);
     delete c;
     return BM_OK;
@@ -498,7 +526,10 @@ bm_status bm_set_stream(bm_ctx* c, void* stream)
     const cudaStream_t s = stream ? (cudaStream_t)stream : c->own_stream;
     // work already queued on the old stream (buffer clears, pattern upload, frames)
     // finishes before anything queued on the new one
-    if (s != c->stream) BM_CUDA(cudaStreamSynchronize(c->stream));
+    if (s != c->stream) {
+        BM_CUDA(cudaStreamSynchronize(c->stream));
+        if (c->refine_stream) BM_CUDA(cudaStreamSynchronize(c->refine_stream));
+    }
     c->stream = s;
     return BM_OK;
 }
@@ -507,6 +538,32 @@ bm_status bm_synchronize(bm_ctx* c)
 {
     if (check_ctx(c)) return BM_ERR_INVALID;
     BM_CUDA(cudaStreamSynchronize(c->stream));
+    if (c->refine_stream) BM_CUDA(cudaStreamSynchronize(c->refine_stream));
+    return BM_OK;
+}
+
+bm_status bm_set_pipelined(bm_ctx* c, int on)
+{
+    if (check_ctx(c)) return BM_ERR_INVALID;
+    if (on && !c->refine_stream) {
+        BM_CUDA(cudaStreamCreateWithFlags(&c->refine_stream, cudaStreamNonBlocking));
+        cudaEvent_t* evs[] = {&c->ev_ready, &c->ev_refined, &c->ev_frame_free[0], &c->ev_frame_free[1],
+                              &c->ev_frame_free[2], &c->ev_flowin_free[0], &c->ev_flowin_free[1]};
+        for (cudaEvent_t* e : evs) BM_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+        // nothing of the refinement stream may start before the work queued so far
+        BM_CUDA(cudaEventRecord(c->ev_ready, c->stream));
+        BM_CUDA(cudaStreamWaitEvent(c->refine_stream, c->ev_ready, 0));
+        BM_CUDA(cudaEventRecord(c->ev_refined, c->refine_stream));
+    }
+    if (!on && c->refine_stream) BM_CUDA(join_refine(c));
+    c->pipelined = on != 0;
+    return BM_OK;
+}
+
+bm_status bm_join(bm_ctx* c)
+{
+    if (check_ctx(c)) return BM_ERR_INVALID;
+    BM_CUDA(join_refine(c));
     return BM_OK;
 }
 
@@ -529,6 +586,7 @@ bm_status bm_read_buffer(bm_ctx* c, bm_buffer_id id, void* dst, size_t bytes, in
     if (st != BM_OK) return st;
     if (!dst) return fail(BM_ERR_INVALID, "bm_read_buffer: null destination");
     if (bytes > cap) return fail(BM_ERR_INVALID, "bm_read_buffer: %zu bytes requested, buffer holds %zu", bytes, cap);
+    BM_CUDA(join_refine(c));
     BM_CUDA(cudaMemcpyAsync(dst, src, bytes, dst_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
                             c->stream));
     if (!dst_on_device) BM_CUDA(cudaStreamSynchronize(c->stream));
@@ -543,6 +601,7 @@ bm_status bm_write_buffer(bm_ctx* c, bm_buffer_id id, const void* src, size_t by
     if (st != BM_OK) return st;
     if (!src) return fail(BM_ERR_INVALID, "bm_write_buffer: null source");
     if (bytes > cap) return fail(BM_ERR_INVALID, "bm_write_buffer: %zu bytes given, buffer holds %zu", bytes, cap);
+    BM_CUDA(join_refine(c));
     BM_CUDA(cudaMemcpyAsync(dst, src, bytes, src_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
                             c->stream));
     if (!src_on_device) BM_CUDA(cudaStreamSynchronize(c->stream));
@@ -566,7 +625,7 @@ bm_status bm_buffer(bm_ctx* c, bm_buffer_id id, void** d_ptr, size_t* bytes)
     case BM_BUF_FLOW_MED: p = c->d_flow_med; b = 2 * ni * 4; break;
     case BM_BUF_FLOW_OUT: p = c->d_flow_out; b = 2 * ni * 4; break;
     case BM_BUF_FRAME: p = c->d_frame[c->cur_frame]; b = ni * 4; break;
-    case BM_BUF_FRAME_PREV: p = c->d_frame[c->cur_frame ^ 1]; b = ni * 4; break;
+    case BM_BUF_FRAME_PREV: p = c->d_frame[c->prev_frame()]; b = ni * 4; break;
     default: return fail(BM_ERR_INVALID, "bm_buffer: unknown id %d", (int)id);
     }
     *d_ptr = p;
@@ -640,12 +699,14 @@ bm_status bm_match(bm_ctx* c, const float* d_im1, const float* d_im2)
 bm_status bm_downsample(bm_ctx* c)
 {
     if (check_ctx(c)) return BM_ERR_INVALID;
+    BM_CUDA(join_refine(c));
     return downsample_impl(c);
 }
 
 bm_status bm_process(bm_ctx* c, const float* d_prev_in)
 {
     if (check_ctx(c)) return BM_ERR_INVALID;
+    BM_CUDA(join_refine(c));
     return process_impl(c, d_prev_in);
 }
 
@@ -660,6 +721,7 @@ bm_status bm_convert(bm_ctx* c, float* h_u, float* h_v)
 {
     if (check_ctx(c)) return BM_ERR_INVALID;
     if (!h_u || !h_v) return fail(BM_ERR_INVALID, "bm_convert: null output");
+    BM_CUDA(join_refine(c));
     const size_t b = c->npix_in * sizeof(float);
     BM_CUDA(cudaMemcpyAsync(h_u, c->d_flow_out, b, cudaMemcpyDeviceToHost, c->stream));
     BM_CUDA(cudaMemcpyAsync(h_v, c->d_flow_out + c->npix_in, b, cudaMemcpyDeviceToHost, c->stream));
@@ -792,12 +854,15 @@ bm_status bm_frame(bm_ctx* c, const uint8_t* frame, int frame_on_device, float* 
     if (!frame) return fail(BM_ERR_INVALID, "bm_frame: null frame");
     const bm_params& p = c->prm;
     const size_t ni = c->npix_in;
+    const int slot = c->cur_frame, prev = c->prev_frame();
+    // a pipelined refinement two frames back may still read this slot as its guide
+    if (c->refine_stream) BM_CUDA(cudaStreamWaitEvent(c->stream, c->ev_frame_free[slot], 0));
     // of_pipeline.cpp:297 (8-bit here: a quarter of the reference's float copy); the
     // frame is kept for the next pair's proposal input
-    uint8_t* d_u8 = c->d_u8[c->cur_frame];
+    uint8_t* d_u8 = c->d_u8[slot];
     BM_CUDA(cudaMemcpyAsync(d_u8, frame, ni, frame_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
                             c->stream));
-    float* cur = c->d_frame[c->cur_frame];
+    float* cur = c->d_frame[slot];
     BM_LAUNCH(c, "u8_to_f32", bmk::u8_to_f32(d_u8, cur, ni, c->stream));
     // of_pipeline.cpp:301-310
     const float* up = cur;
@@ -807,34 +872,66 @@ bm_status bm_frame(bm_ctx* c, const uint8_t* frame, int frame_on_device, float* 
         up = c->d_up;
     }
     bm_status st;
+    bool refine_async = false;
     if (!c->primed) {
         st = features_into(c, up, c->feat2_ptr());
         if (st != BM_OK) return st;
+        BM_CUDA(join_refine(c));
         BM_CUDA(cudaMemsetAsync(c->d_flow_out, 0, 2 * ni * sizeof(float), c->stream));
         c->primed = true;
     } else {
         const bool seeded = c->net != nullptr;
         if (seeded) {
             const uint32_t w4 = p.sx_in / 4, h4 = p.sy_in / 4;
-            st = bm_net_prepare(c->net, 0, c->d_u8[c->cur_frame ^ 1], d_u8, p.sx_in, p.sy_in, c->stream);
+            st = bm_net_prepare(c->net, 0, c->d_u8[prev], d_u8, p.sx_in, p.sy_in, c->stream);
             if (st == BM_OK) st = bm_net_forward(c->net, 1, h4, w4, c->d_pred, c->stream);
             if (st != BM_OK) return st;
             c->launches += 7;
         }
         st = match_impl(c, up, seeded);                           // of_pipeline.cpp:314
-        if (st == BM_OK) st = downsample_impl(c);                 // :319
-        if (st == BM_OK) st = process_impl(c, c->d_frame[c->cur_frame ^ 1]);  // :324
         if (st != BM_OK) return st;
+        if (c->pipelined) {
+            // the down-sampled flow alternates between two buffers; the refinement of
+            // the pair before last must have released this one
+            c->flow_in_slot ^= 1;
+            c->d_flow_in = c->d_flow_in_buf[c->flow_in_slot];
+            BM_CUDA(cudaStreamWaitEvent(c->stream, c->ev_flowin_free[c->flow_in_slot], 0));
+        }
+        st = downsample_impl(c);                                  // :319
+        if (st != BM_OK) return st;
+        if (c->pipelined) {
+            // refinement (:324) and the output copies on the refinement stream, while
+            // the context stream goes on with the next frame
+            BM_CUDA(cudaEventRecord(c->ev_ready, c->stream));
+            BM_CUDA(cudaStreamWaitEvent(c->refine_stream, c->ev_ready, 0));
+            const cudaStream_t main = c->stream;
+            c->stream = c->refine_stream;
+            st = process_impl(c, c->d_frame[prev]);
+            cudaError_t e = cudaSuccess;
+            if (st == BM_OK) {
+                e = cudaEventRecord(c->ev_flowin_free[c->flow_in_slot], c->refine_stream);
+                if (e == cudaSuccess) e = cudaEventRecord(c->ev_frame_free[prev], c->refine_stream);
+            }
+            c->stream = main;
+            if (st != BM_OK) return st;
+            BM_CUDA(e);
+            refine_async = true;
+        } else {
+            st = process_impl(c, c->d_frame[prev]);               // :324
+            if (st != BM_OK) return st;
+        }
     }
     // of_pipeline.cpp:331-333
-    c->cur_frame ^= 1;
+    c->cur_frame = (c->cur_frame + 1) % 3;
     c->feat1 ^= 1;
+    const cudaStream_t out_stream = refine_async ? c->refine_stream : c->stream;
     if (u || v) {
         const cudaMemcpyKind kind = out_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-        if (u) BM_CUDA(cudaMemcpyAsync(u, c->d_flow_out, ni * sizeof(float), kind, c->stream));
-        if (v) BM_CUDA(cudaMemcpyAsync(v, c->d_flow_out + ni, ni * sizeof(float), kind, c->stream));
-        if (!out_on_device) BM_CUDA(cudaStreamSynchronize(c->stream));
+        if (u) BM_CUDA(cudaMemcpyAsync(u, c->d_flow_out, ni * sizeof(float), kind, out_stream));
+        if (v) BM_CUDA(cudaMemcpyAsync(v, c->d_flow_out + ni, ni * sizeof(float), kind, out_stream));
+        if (!out_on_device && !c->pipelined) BM_CUDA(cudaStreamSynchronize(c->stream));
     }
+    if (refine_async) BM_CUDA(cudaEventRecord(c->ev_refined, c->refine_stream));
     return BM_OK;
 }
 

@@ -342,6 +342,20 @@ bm_status bm_frame(bm_ctx* ctx, const uint8_t* frame, int frame_on_device,
 /* Forget the previous frame: the next bm_frame primes again. */
 bm_status bm_reset_sequence(bm_ctx* ctx);
 
+/* Pipelined frames (no counterpart in the reference, which finishes each frame before
+ * the next): with on != 0, bm_frame queues a pair's refinement (median and
+ * cross-trilateral filter) and its output copies on a second stream of the context,
+ * so that they overlap the next frame's up-sampling and matching; results are
+ * identical.  bm_frame then returns without waiting even for host outputs (use
+ * page-locked host memory for them); the outputs of every frame fed so far are
+ * complete after bm_synchronize, or, for work queued behind them on the context
+ * stream, after bm_join.  Other calls that read or write the refinement's buffers
+ * wait for it themselves. */
+bm_status bm_set_pipelined(bm_ctx* ctx, int on);
+/* Make the context stream wait (on the device, without blocking the host) for the
+ * pipelined refinement queued so far; a no-op for a context that never pipelined. */
+bm_status bm_join(bm_ctx* ctx);
+
 /* Count of kernels this context has launched (for launch accounting). */
 uint64_t bm_launch_count(const bm_ctx* ctx);
 
