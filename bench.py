@@ -84,7 +84,8 @@ def parse():
                          "3 = 1920x1080 u4.9 N512 5-frame sequence; 1 and 3 run the plain engine beside the "
                          "reference's own kernels")
     ap.add_argument("--schedule", default=None,
-                    help="ITERATIONS/JFMAX for the learned-seeded engine instead of choosing it by calibration")
+                    help="ITERATIONS/JFMAX[/LOCAL_STEPS] for the learned-seeded engine instead of choosing it by "
+                         "calibration")
     return ap.parse_args()
 
 
@@ -226,7 +227,9 @@ def algorithmic_bytes(kernel, prm):
 
 PROPOSAL_CONF = 0.5
 PIPELINED = True   # each pair's refinement overlaps the next frame (bm_set_pipelined)
-SCHEDULE_CANDIDATES = ((1, 16), (1, 32), (1, 64), (1, 128), (1, 256), (2, 16), (2, 32), (2, 64))
+# (iterations, jfMax, local refinement steps starting at radius 2)
+SCHEDULE_CANDIDATES = tuple((it, jf, ls) for it, jf in ((1, 16), (1, 32), (1, 64), (1, 128), (1, 256), (2, 16), (2, 32),
+                                                       (2, 64)) for ls in (0, 2))
 
 
 def open_engine(torch, prm, pattern, stream, net=None, schedule=None):
@@ -238,6 +241,8 @@ def open_engine(torch, prm, pattern, stream, net=None, schedule=None):
     eng.set_stream(stream.cuda_stream)
     if net is not None:
         bm.set_proposal(eng, net, PROPOSAL_CONF, schedule[0], schedule[1])
+        if len(schedule) > 2 and schedule[2]:
+            bm.set_local_steps(eng, schedule[2], 2)
     if PIPELINED:
         eng.set_pipelined(True)
     return eng
@@ -376,7 +381,7 @@ def choose_schedule(torch, prm, pattern, net, stream):
     best = None
     for sch in SCHEDULE_CANDIDATES:
         ms, epe = run(open_engine(torch, prm, pattern, stream, net, sch))
-        table.append({"schedule": "seeded %d/%d" % sch, "ms": ms, "epe": epe})
+        table.append({"schedule": "seeded %d/%d/ls%d" % sch, "ms": ms, "epe": epe})
         if epe <= plain_epe and (best is None or ms < best[1]):
             best = (sch, ms)
     return (best[0] if best else None), table
@@ -438,7 +443,8 @@ def run_engine(args, torch, world, rank):
     if not args.no_learned and os.path.exists(learn.DEFAULT_WEIGHTS):
         net = learn.load_net(learn.DEFAULT_WEIGHTS, 1, H // 4, W // 4)
         if args.schedule:
-            sch, table = tuple(int(x) for x in args.schedule.split("/")), "given on the command line"
+            sch = tuple(int(x) for x in args.schedule.split("/"))
+            sch, table = (sch + (0,))[:3], "given on the command line"
         else:
             sch, table = choose_schedule(torch, prm, pattern, net, stream)
         learned = {"weights": os.path.relpath(learn.DEFAULT_WEIGHTS, ROOT), "confidence": PROPOSAL_CONF,
@@ -446,7 +452,8 @@ def run_engine(args, torch, world, rank):
         if sch is not None:
             seng = open_engine(torch, prm, pattern, stream, net, sch)
             rl = measure(args, torch, world, seng, d_frames, flows, stream, flush)
-            learned.update({"schedule": {"iterations": sch[0], "jfMax": sch[1]}, "value": rl["value"],
+            learned.update({"schedule": {"iterations": sch[0], "jfMax": sch[1], "local_steps": sch[2]},
+                            "value": rl["value"],
                             "ms_per_step": rl["ms_per_step"], "epe_mean": float(np.mean(rl["epe"])),
                             "speedup_vs_plain": rp["ms_per_step"] / rl["ms_per_step"],
                             "gpu_launches": int(rl["launches"])})
@@ -480,9 +487,7 @@ def run_engine(args, torch, world, rank):
 
     batched = None
     if batch_inputs is not None:
-        bsched = learned["schedule"] if learned and learned.get("schedule") else None
-        batched = run_batched(args, torch, *batch_inputs, net=net if bsched else None,
-                              schedule=(bsched["iterations"], bsched["jfMax"]) if bsched else None)
+        batched = run_batched(args, torch, *batch_inputs, net=net)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -497,6 +502,7 @@ def run_engine(args, torch, world, rank):
         "config": {"workload": WORKLOAD % head_name, "engine": head_name, "width": W, "height": H,
                    "frames_per_step": FRAMES, "pairs_per_step": PAIRS, "upsampling": UP, "feature_length": NBITS,
                    "grid": [prm.sx, prm.sy], "iterations": sched["iterations"], "jfMax": sched["jfMax"],
+                   "local_steps": sched.get("local_steps", 0),
                    "fsize": prm.fsize, "l2": "flushed (256 MB write) before every timed step",
                    "pipelined": PIPELINED,
                    "parallelism": "replicas" if world > 1 else "single GPU"},
@@ -531,25 +537,80 @@ BATCH_SEED = 20261204
 
 
 def _make_batch_pair(args):
-    k, w, h = args
+    seed, w, h = args
     from briefmatch_gb300 import synth
 
-    f0, f1, u, v = synth.make_pair(BATCH_SEED + k, w, h, vmax=15.0)
+    f0, f1, u, v = synth.make_pair(seed, w, h, vmax=15.0)
     return f0, f1, u, v
 
 
-def make_batch_workload(pairs):
-    """64 pairs of uneven size (widths U[320,1920], heights U[240,1080], multiples of
-    4), generated in a spawn-started process pool (before any GPU work)."""
+def make_batch_workload(pairs, seed=None):
+    """Pairs of uneven size (widths U[320,1920], heights U[240,1080], multiples of 4)
+    drawn from `seed` (default: the batched workload's), generated in a
+    spawn-started process pool."""
     import multiprocessing as mp
 
     from briefmatch_gb300 import synth
 
-    sizes = synth.make_batch_sizes(BATCH_SEED, count=pairs)
-    jobs = [(k, w, h) for k, (w, h) in enumerate(sizes)]
+    seed = BATCH_SEED if seed is None else seed
+    sizes = synth.make_batch_sizes(seed, count=pairs)
+    jobs = [(seed + k, w, h) for k, (w, h) in enumerate(sizes)]
     with mp.get_context("spawn").Pool(min(16, os.cpu_count() or 1)) as pool:
         data = pool.map(_make_batch_pair, jobs)
     return sizes, data
+
+
+BATCH_CANDIDATES = ((2, 64, 0), (2, 64, 2), (2, 32, 2), (1, 256, 2), (1, 128, 2))
+
+
+def batch_step_ms_epe(torch, b, data, stream, reps):
+    """Device ms per step and mean EPE of a loaded, scheduled batch."""
+    import numpy as np
+
+    b.run()
+    b.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        b.run()
+    e1.record(stream)
+    b.synchronize()
+    flows = b.read_flows()
+    epe = float(np.mean([np.mean(np.hypot(f[0] - d[2], f[1] - d[3])) for f, d in zip(flows, data)]))
+    return e0.elapsed_time(e1) / reps, epe
+
+
+def choose_batch_schedule(torch, net, stream, pairs=16):
+    """The fastest seeded (iterations, jfMax, local steps) whose mean EPE on a separate
+    calibration batch (other seeds of the same uneven-size generator) is at most the
+    plain batch's there."""
+    import briefmatch_gb300 as bm
+    from briefmatch_gb300.proposal import ProposalNet
+
+    sizes, data = make_batch_workload(pairs, seed=BATCH_SEED + 1000)
+    params = [bm.BMParams.derive(w, h, UP, UP, N=NBITS) for w, h in sizes]
+    b = bm.Batch(params)
+    b.set_stream(stream.cuda_stream)
+    b.load_frames(b.pack_frames([(d[0], d[1]) for d in data]))
+    b.set_schedule(per_pair=1, use_graph=1, streams=2)
+    plain_ms, plain_epe = batch_step_ms_epe(torch, b, data, stream, 2)
+    table = [{"schedule": "plain", "ms": plain_ms, "epe": plain_epe}]
+    bnet = ProposalNet(1, max(h for _, h in sizes) // 4, max(w for w, _ in sizes) // 4)
+    bnet.set_params(net.params())
+    best = None
+    for sch in BATCH_CANDIDATES:
+        b.set_proposal(bnet, PROPOSAL_CONF, sch[0], sch[1])
+        b.set_local_steps(sch[2], 2)
+        b.set_schedule(per_pair=1, use_graph=1, streams=2)
+        ms, epe = batch_step_ms_epe(torch, b, data, stream, 2)
+        table.append({"schedule": "seeded %d/%d/ls%d" % sch, "ms": ms, "epe": epe})
+        if epe <= plain_epe and (best is None or ms < best[1]):
+            best = (sch, ms)
+    b.set_proposal(None)
+    b.close()
+    bnet.close()
+    return (best[0] if best else None), table
 
 
 def run_batched(args, torch, sizes, data, net=None, schedule=None):
@@ -586,12 +647,16 @@ def run_batched(args, torch, sizes, data, net=None, schedule=None):
     epe = float(np.mean([np.mean(np.hypot(f[0] - d[2], f[1] - d[3])) for f, d in zip(flows, data)]))
     sched = b.schedule()
     learned = None
+    calibration = None
     if net is not None:
+        schedule, calibration = choose_batch_schedule(torch, net, stream)
+    if net is not None and schedule is not None:
         from briefmatch_gb300.proposal import ProposalNet
 
         bnet = ProposalNet(1, max(h for _, h in sizes) // 4, max(w for w, _ in sizes) // 4)
         bnet.set_params(net.params())
         b.set_proposal(bnet, PROPOSAL_CONF, schedule[0], schedule[1])
+        b.set_local_steps(schedule[2], 2)
         lrep = b.autotune(None, reps=2)
         for _ in range(args.warmup):
             b.run()
@@ -605,9 +670,10 @@ def run_batched(args, torch, sizes, data, net=None, schedule=None):
         lms = sum(s0.elapsed_time(s1) for s0, s1 in ev) / args.steps
         lflows = b.read_flows()
         lepe = float(np.mean([np.mean(np.hypot(f[0] - d[2], f[1] - d[3])) for f, d in zip(lflows, data)]))
-        learned = {"schedule": {"iterations": schedule[0], "jfMax": schedule[1]}, "value": out_px / (lms * 1e-3) / 1e6,
+        learned = {"schedule": {"iterations": schedule[0], "jfMax": schedule[1], "local_steps": schedule[2]},
+                   "value": out_px / (lms * 1e-3) / 1e6,
                    "ms_per_step": lms, "epe_mean": lepe, "speedup_vs_plain_batch": batch_ms / lms,
-                   "autotune": lrep, "batch_schedule": b.schedule()}
+                   "autotune": lrep, "batch_schedule": b.schedule(), "calibration": calibration}
         b.set_proposal(None)
         bnet.close()
     b.close()
@@ -650,7 +716,8 @@ def run_batched(args, torch, sizes, data, net=None, schedule=None):
         "sequential_value": out_px / (seq_ms * 1e-3) / 1e6, "sequential_ms_per_step": seq_ms,
         "speedup_vs_sequential": seq_ms / batch_ms,
         "schedule": sched, "autotune": report, "epe_mean": epe,
-        "learned": dict(learned, speedup_vs_plain_sequential=seq_ms / learned["ms_per_step"]) if learned else None,
+        "learned": dict(learned, speedup_vs_plain_sequential=seq_ms / learned["ms_per_step"]) if learned else
+        ({"schedule": None, "calibration": calibration} if calibration else None),
     }
 
 

@@ -105,6 +105,9 @@ def _declare(lib):
         "bm_profile_read": (c.c_int, [c.c_void_p, c.c_void_p, c.c_uint32, P(c.c_uint32)]),
         "bm_set_proposal": (c.c_int, [c.c_void_p, c.c_void_p, c.c_float, c.c_uint32, c.c_uint32]),
         "bm_set_pipelined": (c.c_int, [c.c_void_p, c.c_int]),
+        "bm_set_local_steps": (c.c_int, [c.c_void_p, c.c_uint32, c.c_uint32]),
+        "bm_local_step": (c.c_int, [c.c_void_p, c.c_uint32]),
+        "bm_batch_set_local_steps": (c.c_int, [c.c_void_p, c.c_uint32, c.c_uint32]),
         "bm_join": (c.c_int, [c.c_void_p]),
         "bm_batch_set_proposal": (c.c_int, [c.c_void_p, c.c_void_p, c.c_float, c.c_uint32, c.c_uint32]),
         "bm_seed": (c.c_int, [c.c_void_p, c.c_int, c.c_void_p, c.c_uint32, c.c_uint32, c.c_float]),
@@ -502,6 +505,10 @@ class Batch:
     def launch_count(self):
         return int(lib().bm_batch_launch_count(self._b))
 
+    def set_local_steps(self, count, first_radius=2):
+        """Local refinement steps after each pair's seeded initialisation."""
+        check(lib().bm_batch_set_local_steps(self._b, count, first_radius))
+
     def set_proposal(self, net, conf_threshold=0.5, iterations=1, jf_max=16):
         """Seed every pair with a ProposalNet (None detaches); see bm_batch_set_proposal."""
         check(lib().bm_batch_set_proposal(self._b, net.handle if net is not None else None, conf_threshold,
@@ -512,6 +519,16 @@ def set_proposal(engine, net, conf_threshold=0.5, iterations=1, jf_max=16):
     """Attach a ProposalNet (or None) to a BriefMatch context (bm_set_proposal)."""
     check(lib().bm_set_proposal(engine.ctx, net.handle if net is not None else None, conf_threshold, iterations,
                                 jf_max))
+
+
+def set_local_steps(engine, count, first_radius=2):
+    """Local refinement steps after the seeded initialisation (bm_set_local_steps)."""
+    check(lib().bm_set_local_steps(engine.ctx, count, first_radius))
+
+
+def local_step(engine, radius):
+    """One local refinement step on the current field (bm_local_step)."""
+    check(lib().bm_local_step(engine.ctx, radius))
 
 
 def seed(engine, first, d_pred, w4, h4, conf_threshold=0.5):

@@ -109,6 +109,7 @@ struct bm_ctx {
     bm_net* net = nullptr;
     float net_logit_min = 0.0f;
     uint32_t net_iterations = 0, net_jfMax = 0;
+    uint32_t local_steps = 0, local_radius = 1;   // bm_set_local_steps
     float* d_pred = nullptr;   // [h4][w4][3]
 
     struct ProfRec {
@@ -283,6 +284,22 @@ bm_status propagate_pass(bm_ctx* c, int pd, bool fuse_rs, uint32_t jfMax)
     return BM_OK;
 }
 
+// Local refinement steps of the seeded schedule: radius local_radius, then halved
+// down to 1 (bm_set_local_steps).
+bm_status local_steps_impl(bm_ctx* c)
+{
+    const bm_params& p = c->prm;
+    int r = (int)c->local_radius;
+    for (uint32_t k = 0; k < c->local_steps; k++) {
+        BM_LAUNCH(c, "local_step", bmk::local_step(c->feat1_ptr(), c->feat2_ptr(), c->d_flow[c->flow_cur],
+                                                   c->d_flow[c->flow_cur ^ 1], c->d_cost, (int)p.sx, (int)p.sy,
+                                                   (int)c->nsp, r, next_order(c), c->stream));
+        c->flow_cur ^= 1;
+        r = r > 1 ? r / 2 : 1;
+    }
+    return BM_OK;
+}
+
 // BriefMatch::match.  With a proposal network attached (and its prediction in
 // d_pred), the initialisation is the seeded one and the iteration count and jump
 // maximum are the proposal's.
@@ -301,11 +318,14 @@ bm_status match_impl(bm_ctx* c, const float* d_im2, bool seeded)
                                              scy, c->net_logit_min, c->stream));
         iterations = c->net_iterations;
         if (c->net_jfMax) jfMax = c->net_jfMax;
+        c->flow_cur ^= 1;
+        st = local_steps_impl(c);
+        if (st != BM_OK) return st;
     } else {
         BM_LAUNCH(c, "initialize", bmk::initialize(c->feat1_ptr(), c->feat2_ptr(), c->d_flow[c->flow_cur], c->d_flow[c->flow_cur ^ 1],
                                      c->d_cost, (int)p.sx, (int)p.sy, (int)c->nsp, first, next_order(c), c->stream));
+        c->flow_cur ^= 1;
     }
-    c->flow_cur ^= 1;
     int pd = -1;
     for (uint32_t it = 0; it < iterations; it++) {
         st = propagate_pass(c, pd, true, jfMax);
@@ -789,6 +809,28 @@ bm_status bm_set_proposal(bm_ctx* c, bm_net* net, float conf_threshold, uint32_t
     c->net_logit_min = net ? std::log(conf_threshold / (1.0f - conf_threshold)) : 0.0f;
     c->net_iterations = iterations;
     c->net_jfMax = jfMax;
+    return BM_OK;
+}
+
+bm_status bm_set_local_steps(bm_ctx* c, uint32_t count, uint32_t first_radius)
+{
+    if (check_ctx(c)) return BM_ERR_INVALID;
+    if (count > 16 || (count && (first_radius < 1 || first_radius > 256)))
+        return fail(BM_ERR_INVALID, "bm_set_local_steps: at most 16 steps, first radius 1..256");
+    c->local_steps = count;
+    c->local_radius = count ? first_radius : 1;
+    return BM_OK;
+}
+
+bm_status bm_local_step(bm_ctx* c, uint32_t radius)
+{
+    if (check_ctx(c)) return BM_ERR_INVALID;
+    if (radius < 1 || radius > 256) return fail(BM_ERR_INVALID, "bm_local_step: radius 1..256");
+    const bm_params& p = c->prm;
+    BM_LAUNCH(c, "local_step", bmk::local_step(c->feat1_ptr(), c->feat2_ptr(), c->d_flow[c->flow_cur],
+                                               c->d_flow[c->flow_cur ^ 1], c->d_cost, (int)p.sx, (int)p.sy, (int)c->nsp,
+                                               (int)radius, next_order(c), c->stream));
+    c->flow_cur ^= 1;
     return BM_OK;
 }
 

@@ -311,6 +311,7 @@ struct bm_batch {
     bm_net* net = nullptr;
     float net_logit_min = 0.0f;
     uint32_t net_iterations = 0, net_jfMax = 0;
+    uint32_t local_steps = 0, local_radius = 1;   // bm_batch_set_local_steps
     float* d_pred = nullptr;   // [h4][w4][3] of the pair being seeded (pairs run in stream order)
     // concurrent branches of the per-pair schedule (bm_batch_schedule.streams):
     // streams forked from and joined back into the batch stream, and for a proposal
@@ -434,11 +435,21 @@ bm_status enqueue_pair(bm_batch* b, const bm_batch_schedule& s, int j, cudaStrea
         iterations = b->net_iterations;
         if (b->net_jfMax) jfMax = b->net_jfMax;
         b->launches += 8;
+        rev ^= s.snake ? 1 : 0;
+        cur ^= 1;
+        int r = (int)b->local_radius;
+        for (uint32_t k = 0; k < b->local_steps; k++) {
+            BB_CUDA(local_step(d.F[0], d.F[1], d.flow[cur], d.flow[cur ^ 1], d.cost, d.sx, d.sy, (int)b->nsp, r, rev, st));
+            rev ^= s.snake ? 1 : 0;
+            cur ^= 1;
+            r = r > 1 ? r / 2 : 1;
+        }
+        b->launches += b->local_steps;
     } else {
         BB_CUDA(initialize(d.F[0], d.F[1], d.flow[cur], d.flow[cur ^ 1], d.cost, d.sx, d.sy, (int)b->nsp, 1, rev, st));
+        rev ^= s.snake ? 1 : 0;
+        cur ^= 1;
     }
-    rev ^= s.snake ? 1 : 0;
-    cur ^= 1;
     int pd = -1;
     int levels = 0;
     for (int q = (int)jfMax; q > 0; q /= 2) levels++;
@@ -737,7 +748,7 @@ std::string shape_key(const bm_batch* b)
     std::ostringstream ss;
     ss << prop.name << "|pairs=" << b->count << "|N=" << b->N << "|it=" << b->iterations << "|jf=" << b->jfMax
        << "|upMpx=" << (px + 500000) / 1000000;
-    if (b->net) ss << "|seeded=" << b->net_iterations << "/" << b->net_jfMax;
+    if (b->net) ss << "|seeded=" << b->net_iterations << "/" << b->net_jfMax << "/ls" << b->local_steps << "r" << b->local_radius;
     return ss.str();
 }
 
@@ -1134,6 +1145,17 @@ bm_status bm_batch_synchronize(bm_batch* b)
 }
 
 uint64_t bm_batch_launch_count(const bm_batch* b) { return b ? b->launches : 0; }
+
+bm_status bm_batch_set_local_steps(bm_batch* b, uint32_t count, uint32_t first_radius)
+{
+    if (!b) return bfail(BM_ERR_INVALID, "null batch");
+    if (count > 16 || (count && (first_radius < 1 || first_radius > 256)))
+        return bfail(BM_ERR_INVALID, "bm_batch_set_local_steps: at most 16 steps, first radius 1..256");
+    b->local_steps = count;
+    b->local_radius = count ? first_radius : 1;
+    destroy_graph(b);
+    return BM_OK;
+}
 
 bm_status bm_batch_set_proposal(bm_batch* b, bm_net* net, float conf_threshold, uint32_t iterations, uint32_t jfMax)
 {

@@ -417,6 +417,57 @@ __device__ __forceinline__ void jump_px(const uint32_t* __restrict__ F1, const u
     if (h != h0) cost[pix] = (uint16_t)h;
 }
 
+// Local refinement step of the seeded schedule (no reference counterpart): the
+// pixel's own vector moved by r up-sampled pixels left, right, up and down (clamped
+// into the image), in that order, each kept only when strictly cheaper than the
+// best so far.  Reads flow_in (a snapshot) and writes flow_out, like a jump level.
+template <int NSP>
+__device__ __forceinline__ void local_px(const uint32_t* __restrict__ F1, const uint32_t* __restrict__ F2,
+                                         const uint32_t* __restrict__ flow_in, uint32_t* __restrict__ flow_out,
+                                         uint16_t* __restrict__ cost, int sx, int sy, int r, int x, int y)
+{
+    const long pix = x + (long)y * sx;
+    const uint32_t own = __ldg(flow_in + pix);
+    const int h0 = (int)cost[pix];
+    const int ox = lo16(own), oy = hi16(own);
+    uint32_t cand[4];
+    bool live[4];
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        const int dx = c == 0 ? -r : (c == 1 ? r : 0);
+        const int dy = c == 2 ? -r : (c == 3 ? r : 0);
+        const int nx = min(max(ox + dx, -x), sx - x - 1);
+        const int ny = min(max(oy + dy, -y), sy - y - 1);
+        cand[c] = pack_flow(nx, ny);
+        bool dup = cand[c] == own;
+#pragma unroll
+        for (int k = 0; k < c; k++) dup = dup || cand[k] == cand[c];
+        live[c] = !dup;
+    }
+    uint32_t f1[NSP];
+    load_desc_stream<NSP>(f1, F1 + pix * NSP);
+    uint32_t g[4][NSP];
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        const long t = pix + lo16(cand[c]) + (long)hi16(cand[c]) * sx;
+        gather_desc_pred<NSP>(g[c], F2 + t * NSP, live[c]);
+    }
+    int h = h0;
+    uint32_t best = own;
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        int acc = 0;
+#pragma unroll
+        for (int k = 0; k < NSP; k++) acc += __popc(f1[k] ^ g[c][k]);
+        if (live[c] && acc < h) {
+            h = acc;
+            best = cand[c];
+        }
+    }
+    flow_out[pix] = best;
+    if (h != h0) cost[pix] = (uint16_t)h;
+}
+
 // ---------------------------------------------------------------------------
 // Down-sampling (briefmatch.cpp:296-324) for input-resolution pixel (x, y):
 // int16 -> float, Gaussian H then V evaluated only where the nearest-neighbour

@@ -61,6 +61,9 @@ cudaError_t seed_field(const uint32_t* F1, const uint32_t* F2, const uint32_t* f
                        uint16_t* cost, int sx, int sy, int nsp, int first, const float* pred, int w4, int h4,
                        float scale_x, float scale_y, float logit_min, cudaStream_t st);
 
+cudaError_t local_step(const uint32_t* F1, const uint32_t* F2, const uint32_t* flow_in, uint32_t* flow_out,
+                       uint16_t* cost, int sx, int sy, int nsp, int r, int rev, cudaStream_t st);
+
 cudaError_t jump_level(const uint32_t* F1, const uint32_t* F2, const uint32_t* flow_in,
                        uint32_t* flow_out, uint16_t* cost, int sx, int sy, int nsp,
                        int p, int pd, int doubleProp, const RsArgs& rs, int rev, cudaStream_t st);

@@ -132,6 +132,17 @@ __global__ void __launch_bounds__(256) k_jump_level(const uint32_t* __restrict__
 }
 
 template <int NSP>
+__global__ void __launch_bounds__(256) k_local_step(const uint32_t* __restrict__ F1, const uint32_t* __restrict__ F2,
+                                                    const uint32_t* __restrict__ flow_in, uint32_t* __restrict__ flow_out,
+                                                    uint16_t* __restrict__ cost, int sx, int sy, int r, int rev)
+{
+    const int2 t0 = block_tile(rev);
+    const int x = t0.x + threadIdx.x, y = t0.y + threadIdx.y;
+    if (x >= sx || y >= sy) return;
+    local_px<NSP>(F1, F2, flow_in, flow_out, cost, sx, sy, r, x, y);
+}
+
+template <int NSP>
 __global__ void __launch_bounds__(256) k_random_search(const uint32_t* __restrict__ F1, const uint32_t* __restrict__ F2,
                                                        uint32_t* __restrict__ flow, uint16_t* __restrict__ cost,
                                                        int sx, int sy, RsArgs rs)
@@ -353,6 +364,13 @@ cudaError_t jump_level(const uint32_t* F1, const uint32_t* F2, const uint32_t* f
     } else {
         BM_DISPATCH_NSP(nsp, k_jump_level<NSP, false><<<grid2d(sx, sy), dim3(TX, TY), 0, st>>>(F1, F2, flow_in, flow_out, cost, sx, sy, p, pd, doubleProp, rs, rev));
     }
+    return cudaGetLastError();
+}
+
+cudaError_t local_step(const uint32_t* F1, const uint32_t* F2, const uint32_t* flow_in, uint32_t* flow_out,
+                       uint16_t* cost, int sx, int sy, int nsp, int r, int rev, cudaStream_t st)
+{
+    BM_DISPATCH_NSP(nsp, k_local_step<NSP><<<grid2d(sx, sy), dim3(TX, TY), 0, st>>>(F1, F2, flow_in, flow_out, cost, sx, sy, r, rev));
     return cudaGetLastError();
 }
 

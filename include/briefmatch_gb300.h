@@ -255,6 +255,8 @@ bm_status bm_batch_autotune(bm_batch* b, const char* cache_path, int reps, char*
  * used on another stream while the batch runs. */
 typedef struct bm_net bm_net;
 bm_status bm_batch_set_proposal(bm_batch* b, bm_net* net, float conf_threshold, uint32_t iterations, uint32_t jfMax);
+/* Local refinement steps after each pair's seeded initialisation (bm_set_local_steps). */
+bm_status bm_batch_set_local_steps(bm_batch* b, uint32_t count, uint32_t first_radius);
 
 /* Self-test of the bounded grid barrier: `blocks` co-resident blocks wait for `expect`
  * arrivals for at most spin_limit polls each.  With expect > blocks nobody can pass:
@@ -303,6 +305,16 @@ bm_status bm_set_proposal(bm_ctx* ctx, bm_net* net, float conf_threshold, uint32
  * (d_pred [h4][w4][3]: u, v in cell units, confidence logit) where the confidence
  * reaches conf_threshold -- kept only if its Hamming cost is strictly lower. */
 bm_status bm_seed(bm_ctx* ctx, int first, const float* d_pred, uint32_t w4, uint32_t h4, float conf_threshold);
+
+/* Local refinement steps of the seeded schedule (no counterpart in the reference):
+ * after the seeded initialisation, `count` steps each try the pixel's own vector moved
+ * by r up-sampled pixels left, right, up and down (clamped into the image), keeping a
+ * candidate only if its Hamming cost is strictly lower than the best so far; r starts
+ * at first_radius and halves down to 1.  Applies to matching seeded by the proposal
+ * (bm_set_proposal); 0 steps (the default) leaves the seeded schedule as it was. */
+bm_status bm_set_local_steps(bm_ctx* ctx, uint32_t count, uint32_t first_radius);
+/* One local refinement step of radius r on the current field (the stage entry point). */
+bm_status bm_local_step(bm_ctx* ctx, uint32_t radius);
 
 /* ---- refinement without allocation ------------------------------------------------ */
 

@@ -136,6 +136,30 @@ def seed(F1, F2, sx, sy, N, first, pred, w4, h4, scale_x, scale_y, logit_min, NX
     return NX, NY, H
 
 
+def local_step(F1, F2, sx, sy, N, r, NX, NY, H):
+    """Local refinement step of the seeded schedule (no reference counterpart): each
+    pixel's own vector moved by r left, right, up and down (clamped into the image),
+    in that order, each kept only if strictly cheaper than the best so far; all
+    pixels read the same snapshot."""
+    F1 = _c(F1, np.uint32)
+    F2 = _c(F2, np.uint32)
+    NX = _c(NX, np.int16).astype(np.int64)
+    NY = _c(NY, np.int16).astype(np.int64)
+    best_x, best_y, best_h = NX.copy(), NY.copy(), _c(H, np.uint16).astype(np.int64)
+    ys, xs = np.mgrid[0:sy, 0:sx]
+    xs, ys = xs.ravel(), ys.ravel()
+    pix = np.arange(sx * sy)
+    for dx, dy in ((-r, 0), (r, 0), (0, -r), (0, r)):
+        tx = np.clip(NX + dx, -xs, sx - xs - 1)
+        ty = np.clip(NY + dy, -ys, sy - ys - 1)
+        h = _hamming_rows(F1, F2[pix + tx + ty * sx])
+        win = h < best_h
+        best_x = np.where(win, tx, best_x)
+        best_y = np.where(win, ty, best_y)
+        best_h = np.where(win, h, best_h)
+    return best_x.astype(np.int16), best_y.astype(np.int16), best_h.astype(np.uint16)
+
+
 def jump_level(F1, F2, sx, sy, N, p, pd, double_prop, NX, NY, H):
     NXs = _c(NX, np.int16).copy()
     NYs = _c(NY, np.int16).copy()
@@ -245,11 +269,12 @@ class Sequence:
     to take libm-vs-fast-math Lanczos differences out of a comparison);
     ``normals_fn(call, n)`` supplies the random-search normals of call ``call``;
     ``nn`` the device's down-sampling index tables (see ``downsample``).
-    ``proposal`` = (pred_fn, logit_min, iterations, jf_max) switches matching to
-    the seeded schedule: pred_fn(prev_u8, cur_u8) gives the [h4][w4][3]
-    quarter-resolution proposal, ``seed`` replaces the plain initialisation and
-    the proposal's iteration count and jump maximum replace the parameters'
-    (jf_max 0 keeps them)."""
+    ``proposal`` = (pred_fn, logit_min, iterations, jf_max[, local_radii])
+    switches matching to the seeded schedule: pred_fn(prev_u8, cur_u8) gives the
+    [h4][w4][3] quarter-resolution proposal, ``seed`` replaces the plain
+    initialisation, one ``local_step`` follows per radius in local_radii, and the
+    proposal's iteration count and jump maximum replace the parameters' (jf_max 0
+    keeps them)."""
 
     def __init__(self, params: dict, pattern, normals_fn, nn=None, proposal=None):
         self.proposal = proposal
@@ -283,7 +308,8 @@ class Sequence:
                 NX, NY, H = match(self.F1, F2, sx, sy, N, it, p["jfMax"], p["doubleProp"], first, search_dist(sx), nrm,
                                   self.NX, self.NY)
             else:
-                pred_fn, logit_min, it, jf = self.proposal
+                pred_fn, logit_min, it, jf = self.proposal[:4]
+                radii = self.proposal[4] if len(self.proposal) > 4 else ()
                 jf = jf or p["jfMax"]
                 w4, h4 = sxi // 4, syi // 4
                 f32 = np.float32
@@ -291,6 +317,8 @@ class Sequence:
                 scy = f32(4.0) * f32(sy) / f32(syi)
                 pred = pred_fn(self.prev_u8, frame_u8)
                 NX, NY, H = seed(self.F1, F2, sx, sy, N, first, pred, w4, h4, scx, scy, logit_min, self.NX, self.NY)
+                for r in radii:
+                    NX, NY, H = local_step(self.F1, F2, sx, sy, N, r, NX, NY, H)
                 pd = -1
                 for k in range(it):
                     NX, NY, H = propagate(self.F1, F2, sx, sy, N, pd, jf, p["doubleProp"], NX, NY, H)

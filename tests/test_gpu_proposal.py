@@ -11,7 +11,7 @@ import pytest
 
 import briefmatch_gb300 as bm
 import oracle
-from bmtest import engine_field, engine_normals, make_engine, random_field, set_field, small_params
+from bmtest import engine_field, engine_normals, hamming_at, make_engine, random_field, set_field, small_params
 
 pytestmark = pytest.mark.gpu
 
@@ -73,6 +73,22 @@ def test_seed_matches_oracle(first):
     assert (cost <= H0).all() and (cost < H0).any()
 
 
+@pytest.mark.parametrize("r", [1, 3])
+def test_local_step_matches_oracle(r):
+    prm = small_params(96, 64, 1.5, 1.5, N=64)
+    eng, pattern = make_engine(prm)
+    F1, F2 = _features(eng, prm, pattern, seed=23)
+    rng = np.random.default_rng(r)
+    NX0, NY0 = random_field(rng, prm.sx, prm.sy, 6)
+    H0 = hamming_at(F1, F2, prm.sx, NX0, NY0)
+    set_field(eng, NX0, NY0, H0)
+    bm.local_step(eng, r)
+    nx, ny, cost, _ = engine_field(eng)
+    NX, NY, H = oracle.local_step(F1, F2, prm.sx, prm.sy, prm.N, r, NX0, NY0, H0)
+    assert np.array_equal(nx, NX) and np.array_equal(ny, NY) and np.array_equal(cost, H)
+    assert (cost <= H0).all() and (cost < H0).any()
+
+
 def test_seed_rejects_bad_arguments():
     prm = small_params(64, 48)
     eng, _ = make_engine(prm)
@@ -93,7 +109,8 @@ def _net_with_spread_logits(h4, w4, seed=3):
     return net
 
 
-def test_seeded_sequence_matches_oracle():
+@pytest.mark.parametrize("local", [(), (2, 1)])
+def test_seeded_sequence_matches_oracle(local):
     W, H = 88, 64
     prm = small_params(W, H, 2.0, 2.0, N=64)
     eng, pattern = make_engine(prm, pattern_seed=4)
@@ -101,6 +118,8 @@ def test_seeded_sequence_matches_oracle():
     net = _net_with_spread_logits(h4, w4)
     it, jf = 1, 8
     bm.set_proposal(eng, net, 0.5, it, jf)
+    if local:
+        bm.set_local_steps(eng, len(local), local[0])
 
     def pred_fn(prev_u8, cur_u8):
         d0, d1 = _dev(prev_u8), _dev(cur_u8)
@@ -120,7 +139,8 @@ def test_seeded_sequence_matches_oracle():
             normals_cache[call] = engine_normals(eng, call)
         return normals_cache[call]
 
-    seq = oracle.Sequence(prm.as_dict(), pattern, normals_fn, nn=eng.nn_indices(), proposal=(pred_fn, 0.0, it, jf))
+    seq = oracle.Sequence(prm.as_dict(), pattern, normals_fn, nn=eng.nn_indices(),
+                          proposal=(pred_fn, 0.0, it, jf, local))
     frames, _ = synth.make_sequence(8, W, H, 4, vmax=5.0)
     for k, f in enumerate(frames):
         d = _dev(f)
@@ -175,6 +195,7 @@ def test_batch_seeded_equals_single_contexts():
         eng.clean()
     b = bm.Batch(params)
     b.set_proposal(net, 0.5, 1, 8)
+    b.set_local_steps(0, 1)
     with pytest.raises(bm.BriefMatchException):
         b.set_schedule(per_pair=0)
     for use_graph, streams in ((0, 1), (1, 1), (1, 2), (0, 3)):
@@ -184,6 +205,31 @@ def test_batch_seeded_equals_single_contexts():
         b.synchronize()
         for k, ((gu, gv), (wu, wv)) in enumerate(zip(b.read_flows(), want)):
             assert np.array_equal(gu, wu) and np.array_equal(gv, wv), (use_graph, k)
+    b.close()
+
+
+def test_batch_local_steps_equal_single_contexts():
+    sizes = [(96, 64), (72, 56)]
+    params = [small_params(w, h, 2.0, 2.0, N=64) for w, h in sizes]
+    frames = [synth.make_pair(70 + k, w, h, 5.0)[:2] for k, (w, h) in enumerate(sizes)]
+    net = _net_with_spread_logits(max(h for _, h in sizes) // 4, max(w for w, _ in sizes) // 4)
+    want = []
+    for p, (f0, f1) in zip(params, frames):
+        eng = bm.FlowEngine(p)
+        bm.set_proposal(eng, net, 0.5, 1, 8)
+        bm.set_local_steps(eng, 2, 2)
+        eng.process_frame(f0)
+        want.append(eng.process_frame(f1))
+        eng.clean()
+    b = bm.Batch(params)
+    b.set_proposal(net, 0.5, 1, 8)
+    b.set_local_steps(2, 2)
+    b.set_schedule(per_pair=1, use_graph=1, streams=2)
+    b.load_frames(b.pack_frames(frames))
+    b.run()
+    b.synchronize()
+    for k, ((gu, gv), (wu, wv)) in enumerate(zip(b.read_flows(), want)):
+        assert np.array_equal(gu, wu) and np.array_equal(gv, wv), k
     b.close()
 
 
