@@ -1,7 +1,7 @@
 """Training and evaluation of the learned flow proposal.
 
-  python -m briefmatch_gb300.learn train --pairs 10000 --out briefmatch_gb300/weights/proposal.f32
-  python -m briefmatch_gb300.learn eval --weights briefmatch_gb300/weights/proposal.f32
+  python -m briefmatch_gb300.learn train [--pairs 30000 --epochs 50 --out PATH]
+  python -m briefmatch_gb300.learn eval [--weights PATH]
 
 Training data: seeded synthetic 512x384 pairs (briefmatch_gb300.synth); targets:
 the flow BriefMatch itself computes for each pair (the engine with 4 iterations, the
@@ -292,8 +292,8 @@ def main(argv=None):
     ap = argparse.ArgumentParser()
     sub = ap.add_subparsers(dest="cmd", required=True)
     t = sub.add_parser("train")
-    t.add_argument("--pairs", type=int, default=10000)
-    t.add_argument("--epochs", type=int, default=3)
+    t.add_argument("--pairs", type=int, default=30000)
+    t.add_argument("--epochs", type=int, default=50)
     t.add_argument("--batch", type=int, default=32)
     t.add_argument("--lr", type=float, default=2e-3)
     t.add_argument("--seed", type=int, default=1)
