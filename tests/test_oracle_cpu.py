@@ -181,3 +181,69 @@ def test_epe():
 def test_search_dist():
     # briefmatch.cpp:271
     assert oracle.search_dist(2969) == np.float32(np.sqrt(np.ceil(np.float32(2969) * np.float32(0.5) / np.float32(3))))
+
+
+def _pix_hamming(F1, F2, p, q):
+    return int(sum(bin(int(a) ^ int(b)).count("1") for a, b in zip(F1[p], F2[q])))
+
+
+def _setup_pair(seed, sx, sy, N):
+    rng = np.random.default_rng(seed)
+    pattern = np.clip(rng.normal(0, 4, 4 * N), -12, 12).astype(np.float32)
+    F1 = oracle.features(random_image(rng, sx, sy), pattern, N)
+    F2 = oracle.features(random_image(rng, sx, sy), pattern, N)
+    return rng, F1, F2
+
+
+@pytest.mark.parametrize("first", [True, False])
+def test_seed_against_python(first):
+    """oracle.seed (vectorised) against a per-pixel loop of the seeding rule."""
+    sx, sy, N = 23, 17, 64
+    rng, F1, F2 = _setup_pair(5, sx, sy, N)
+    NX0, NY0 = random_field(rng, sx, sy, 5) if not first else (None, None)
+    w4, h4 = 6, 5
+    pred = np.zeros((h4, w4, 3), np.float32)
+    pred[..., :2] = rng.uniform(-2, 2, (h4, w4, 2))
+    pred[..., 2] = rng.choice([-1.0, 1.0], (h4, w4))
+    scx, scy = np.float32(sx) / np.float32(w4), np.float32(sy) / np.float32(h4)
+    NX, NY, H = oracle.seed(F1, F2, sx, sy, N, first, pred, w4, h4, scx, scy, 0.0, NX0, NY0)
+    IX, IY, IH = oracle.initialize(F1, F2, sx, sy, N, first, NX0, NY0)
+    for y in range(sy):
+        for x in range(sx):
+            p = y * sx + x
+            bx, by, bh = int(IX[p]), int(IY[p]), int(IH[p])
+            qx = min(w4 - 1, max(0, int((np.float32(x) + np.float32(0.5)) * (np.float32(1) / scx))))
+            qy = min(h4 - 1, max(0, int((np.float32(y) + np.float32(0.5)) * (np.float32(1) / scy))))
+            u, v, c = pred[qy, qx]
+            if c >= 0:
+                cx = min(max(int(np.rint(u * scx)), -x), sx - x - 1)
+                cy = min(max(int(np.rint(v * scy)), -y), sy - y - 1)
+                if (cx, cy) != (bx, by):
+                    h = _pix_hamming(F1, F2, p, p + cx + cy * sx)
+                    if h < bh:
+                        bx, by, bh = cx, cy, h
+            assert (NX[p], NY[p], H[p]) == (bx, by, bh), (x, y)
+
+
+@pytest.mark.parametrize("r", [1, 2])
+def test_local_step_against_python(r):
+    """oracle.local_step (vectorised) against a per-pixel loop: the own vector moved by
+    r left, right, up, down (clamped), strictly-better accept in that order."""
+    sx, sy, N = 21, 15, 32
+    rng, F1, F2 = _setup_pair(7, sx, sy, N)
+    NX0, NY0 = random_field(rng, sx, sy, 4)
+    H0 = hamming_at(F1, F2, sx, NX0, NY0)
+    NX, NY, H = oracle.local_step(F1, F2, sx, sy, N, r, NX0, NY0, H0)
+    for y in range(sy):
+        for x in range(sx):
+            p = y * sx + x
+            bx, by, bh = int(NX0[p]), int(NY0[p]), int(H0[p])
+            ox, oy = bx, by
+            for dx, dy in ((-r, 0), (r, 0), (0, -r), (0, r)):
+                cx = min(max(ox + dx, -x), sx - x - 1)
+                cy = min(max(oy + dy, -y), sy - y - 1)
+                h = _pix_hamming(F1, F2, p, p + cx + cy * sx)
+                if h < bh:
+                    bx, by, bh = cx, cy, h
+            assert (NX[p], NY[p], H[p]) == (bx, by, bh), (x, y)
+    assert (H <= H0).all()
