@@ -66,7 +66,14 @@ struct bm_ctx {
     float* d_frame[3] = {nullptr, nullptr, nullptr};
     int cur_frame = 0;
     int prev_frame() const { return (cur_frame + 2) % 3; }
-    float* d_up = nullptr;
+    float* d_up = nullptr;   // dense up-sampled image (BM_BUF_UP), filled on request
+    // working up-sampled image with an edge-replicated margin of up_margin pixels on
+    // every side (at least the pattern's largest offset), row pitch up_pitch()
+    float* d_upad = nullptr;
+    int up_margin = 0;
+    bool upad_valid = false;   // d_upad holds the current frame
+    int up_pitch() const { return (int)prm.sx + 2 * up_margin; }
+    float* upad_origin() const { return d_upad + (size_t)up_margin * up_pitch() + up_margin; }
     uint32_t* d_feat[2] = {nullptr, nullptr};
     int feat1 = 0;                           // d_feat[feat1] is FEAT1, d_feat[feat1^1] FEAT2
     uint32_t* d_flow[2] = {nullptr, nullptr};
@@ -88,7 +95,8 @@ struct bm_ctx {
     float* d_tmp = nullptr;
     int4* d_pattern = nullptr;
     int pattern_rmax = 0;
-    bmk::PatternOffsets pattern_off;   // linear offsets for width sx
+    bmk::PatternOffsets pattern_off;       // linear offsets for width sx
+    bmk::PatternOffsets pattern_off_pad;   // linear offsets for pitch up_pitch()
     float* d_taps = nullptr;
     float* d_lx = nullptr;
     int* d_ix = nullptr;
@@ -198,7 +206,7 @@ bm_status dev_alloc(T** p, size_t count)
 
 void release(bm_ctx* c)
 {
-    void* ptrs[] = {c->d_u8[0], c->d_u8[1], c->d_u8[2], c->d_pred, c->d_frame[0], c->d_frame[1], c->d_frame[2], c->d_up,
+    void* ptrs[] = {c->d_u8[0], c->d_u8[1], c->d_u8[2], c->d_pred, c->d_frame[0], c->d_frame[1], c->d_frame[2], c->d_up, c->d_upad,
                     c->d_feat[0], c->d_feat[1], c->d_flow[0], c->d_flow[1], c->d_cost, c->d_flow_in_buf[0],
                     c->d_flow_in_buf[1], c->d_flow_med, c->d_flow_out,
                     c->d_tmp, c->d_pattern, c->d_taps, c->d_lx, c->d_ix, c->d_ly, c->d_iy,
@@ -249,9 +257,14 @@ bmk::RsArgs rs_args(const bm_ctx* c, bool enabled)
     return rs;
 }
 
-bm_status features_into(bm_ctx* c, const float* d_up, uint32_t* F)
+bm_status features_into(bm_ctx* c, const float* d_up, uint32_t* F, bool padded = false)
 {
     const bm_params& p = c->prm;
+    if (padded) {
+        BM_LAUNCH(c, "features", bmk::features_pad(d_up, c->up_pitch(), F, (int)p.sx, (int)p.sy, (int)c->nsp,
+                                                   c->pattern_off_pad, next_order(c), c->stream));
+        return BM_OK;
+    }
     BM_LAUNCH(c, "features", bmk::features(d_up, F, (int)p.sx, (int)p.sy, (int)p.N, (int)c->nsp, c->d_pattern, c->pattern_rmax,
                                c->pattern_off, next_order(c), c->stream));
     return BM_OK;
@@ -303,10 +316,10 @@ bm_status local_steps_impl(bm_ctx* c)
 // BriefMatch::match.  With a proposal network attached (and its prediction in
 // d_pred), the initialisation is the seeded one and the iteration count and jump
 // maximum are the proposal's.
-bm_status match_impl(bm_ctx* c, const float* d_im2, bool seeded)
+bm_status match_impl(bm_ctx* c, const float* d_im2, bool seeded, bool padded = false)
 {
     const bm_params& p = c->prm;
-    bm_status st = features_into(c, d_im2, c->feat2_ptr());
+    bm_status st = features_into(c, d_im2, c->feat2_ptr(), padded);
     if (st != BM_OK) return st;
     const int first = (c->first_match || !p.tInit) ? 1 : 0;
     uint32_t iterations = p.iterations, jfMax = p.jfMax;
@@ -388,10 +401,27 @@ bm_status set_pattern_impl(bm_ctx* c, const float* h_pattern)
         }
         pat[s] = make_int4(v[0], v[1], v[2], v[3]);
     }
+    // the working up-sampled image's margin must cover the largest offset
+    const bm_params& p = c->prm;
+    if ((p.sx != p.sx_in || p.sy != p.sy_in) && (!c->d_upad || rmax > c->up_margin)) {
+        BM_CUDA(cudaStreamSynchronize(c->stream));
+        if (c->d_upad) BM_CUDA(cudaFree(c->d_upad));
+        c->d_upad = nullptr;
+        c->upad_valid = false;
+        c->up_margin = rmax;
+        const bm_status st = dev_alloc(&c->d_upad, (size_t)c->up_pitch() * (p.sy + 2 * (size_t)rmax));
+        if (st != BM_OK) {
+            c->up_margin = 0;
+            return st;
+        }
+    }
     std::memset(&c->pattern_off, 0, sizeof(c->pattern_off));
-    const int sx = (int)c->prm.sx;
-    for (uint32_t s = 0; s < N; s++)
+    std::memset(&c->pattern_off_pad, 0, sizeof(c->pattern_off_pad));
+    const int sx = (int)p.sx, pitch = c->up_pitch();
+    for (uint32_t s = 0; s < N; s++) {
         c->pattern_off.off[s] = make_int2(pat[s].x + pat[s].y * sx, pat[s].z + pat[s].w * sx);
+        c->pattern_off_pad.off[s] = make_int2(pat[s].x + pat[s].y * pitch, pat[s].z + pat[s].w * pitch);
+    }
     BM_CUDA(cudaMemcpyAsync(c->d_pattern, pat.data(), N * sizeof(int4), cudaMemcpyHostToDevice, c->stream));
     BM_CUDA(cudaStreamSynchronize(c->stream));
     c->pattern_rmax = rmax;
@@ -640,7 +670,15 @@ bm_status bm_buffer(bm_ctx* c, bm_buffer_id id, void** d_ptr, size_t* bytes)
     case BM_BUF_FEAT2: p = c->feat2_ptr(); b = n * c->nsp * 4; break;
     case BM_BUF_FLOW: p = c->d_flow[c->flow_cur]; b = n * 4; break;
     case BM_BUF_COST: p = c->d_cost; b = n * 2; break;
-    case BM_BUF_UP: p = c->d_up; b = n * 4; break;
+    case BM_BUF_UP:
+        if (c->upad_valid) {   // the dense copy of the working (edge-replicated) image
+            const size_t w = (size_t)c->prm.sx * sizeof(float);
+            BM_CUDA(cudaMemcpy2DAsync(c->d_up, w, c->upad_origin(), (size_t)c->up_pitch() * sizeof(float), w,
+                                      c->prm.sy, cudaMemcpyDeviceToDevice, c->stream));
+        }
+        p = c->d_up;
+        b = n * 4;
+        break;
     case BM_BUF_FLOW_IN: p = c->d_flow_in; b = 2 * ni * 4; break;
     case BM_BUF_FLOW_MED: p = c->d_flow_med; b = 2 * ni * 4; break;
     case BM_BUF_FLOW_OUT: p = c->d_flow_out; b = 2 * ni * 4; break;
@@ -908,15 +946,18 @@ bm_status bm_frame(bm_ctx* c, const uint8_t* frame, int frame_on_device, float* 
     BM_LAUNCH(c, "u8_to_f32", bmk::u8_to_f32(d_u8, cur, ni, c->stream));
     // of_pipeline.cpp:301-310
     const float* up = cur;
-    if (p.sx != p.sx_in || p.sy != p.sy_in) {
-        BM_LAUNCH(c, "upsample_u8", bmk::upsample_u8(d_u8, c->d_up, (int)p.sx_in, (int)p.sy_in, (int)p.sx, (int)p.sy, c->d_lx, c->d_ix,
-                                      c->d_ly, c->d_iy, c->stream));
-        up = c->d_up;
+    const bool padded = p.sx != p.sx_in || p.sy != p.sy_in;
+    if (padded) {
+        BM_LAUNCH(c, "upsample_u8", bmk::upsample_u8_pad(d_u8, c->d_upad, c->up_pitch(), c->up_margin, (int)p.sx_in,
+                                                         (int)p.sy_in, (int)p.sx, (int)p.sy, c->d_lx, c->d_ix, c->d_ly,
+                                                         c->d_iy, c->stream));
+        up = c->upad_origin();
+        c->upad_valid = true;
     }
     bm_status st;
     bool refine_async = false;
     if (!c->primed) {
-        st = features_into(c, up, c->feat2_ptr());
+        st = features_into(c, up, c->feat2_ptr(), padded);
         if (st != BM_OK) return st;
         BM_CUDA(join_refine(c));
         BM_CUDA(cudaMemsetAsync(c->d_flow_out, 0, 2 * ni * sizeof(float), c->stream));
@@ -930,7 +971,7 @@ bm_status bm_frame(bm_ctx* c, const uint8_t* frame, int frame_on_device, float* 
             if (st != BM_OK) return st;
             c->launches += 7;
         }
-        st = match_impl(c, up, seeded);                           // of_pipeline.cpp:314
+        st = match_impl(c, up, seeded, padded);                   // of_pipeline.cpp:314
         if (st != BM_OK) return st;
         if (c->pipelined) {
             // the down-sampled flow alternates between two buffers; the refinement of

@@ -162,9 +162,9 @@ __device__ __forceinline__ f2x ex2_2(f2x a) { return pk2(exp2f(lo2(a)), exp2f(hi
 // accumulation runs in the reference's order (i outer, j inner).
 // ---------------------------------------------------------------------------
 template <typename T>
-__device__ __forceinline__ void upsample_px(const T* __restrict__ in, float* __restrict__ out, int sxi, int syi,
-                                            int sxo, const float* __restrict__ lx, const int* __restrict__ ix,
-                                            const float* __restrict__ ly, const int* __restrict__ iy, int x, int y)
+__device__ __forceinline__ float upsample_val(const T* __restrict__ in, int sxi, int syi,
+                                              const float* __restrict__ lx, const int* __restrict__ ix,
+                                              const float* __restrict__ ly, const int* __restrict__ iy, int x, int y)
 {
     int x1 = ix[x], y1 = iy[y];
     float Ly[6];
@@ -185,7 +185,15 @@ __device__ __forceinline__ void upsample_px(const T* __restrict__ in, float* __r
             v += float(in[ci + row[b]]) * Lx * Ly[b];
         }
     }
-    out[x + (size_t)y * sxo] = v / w;
+    return v / w;
+}
+
+template <typename T>
+__device__ __forceinline__ void upsample_px(const T* __restrict__ in, float* __restrict__ out, int sxi, int syi,
+                                            int sxo, const float* __restrict__ lx, const int* __restrict__ ix,
+                                            const float* __restrict__ ly, const int* __restrict__ iy, int x, int y)
+{
+    out[x + (size_t)y * sxo] = upsample_val<T>(in, sxi, syi, lx, ix, ly, iy, x, y);
 }
 
 // ---------------------------------------------------------------------------
@@ -215,6 +223,44 @@ __device__ __forceinline__ void features_interior_px(const float* __restrict__ I
         word[wd] = acc;
     }
     store_desc<NSP>(F + ((size_t)y * sx + x) * NSP, word);
+}
+
+// A strip of PX pixels at x, x+TX, ..., x+(PX-1)*TX of one row, in an image whose
+// every sample point of those pixels is addressable (an edge-replicated margin at
+// least as wide as the largest offset: the reads then equal the reference's
+// per-coordinate clamped reads).  `base` points at pixel x, `room` = sx - x; the
+// strip's pixels share each offset's address arithmetic (the others are immediate
+// displacements of TX pixels).
+template <int NSP, int PX, typename OffArray>
+__device__ __forceinline__ void features_strip_px(const float* __restrict__ base, uint32_t* __restrict__ F, int room,
+                                                  const OffArray& off)
+{
+    uint32_t word[PX][NSP];
+#pragma unroll
+    for (int wd = 0; wd < NSP; wd++) {
+        uint32_t acc[PX];
+#pragma unroll
+        for (int k = 0; k < PX; k++) acc[k] = 0;
+#pragma unroll
+        for (int b = 0; b < 32; b++) {
+            const int2 o = off[wd * 32 + b];
+            const float* p1 = base + o.x;
+            const float* p2 = base + o.y;
+#pragma unroll
+            for (int k = 0; k < PX; k++) {
+                if (k == 0 || k * TX < room) {
+                    const float i1 = __ldg(p1 + k * TX);
+                    const float i2 = __ldg(p2 + k * TX);
+                    if (i1 > i2) acc[k] |= 1u << b;
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < PX; k++) word[k][wd] = acc[k];
+    }
+#pragma unroll
+    for (int k = 0; k < PX; k++)
+        if (k == 0 || k * TX < room) store_desc<NSP>(F + (size_t)k * TX * NSP, word[k]);
 }
 
 template <int NSP>

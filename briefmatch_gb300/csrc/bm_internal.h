@@ -41,6 +41,10 @@ cudaError_t upsample_f32(const float* in, float* out, int sxi, int syi, int sxo,
                          const float* lx, const int* ix, const float* ly, const int* iy, cudaStream_t st);
 cudaError_t upsample_u8(const uint8_t* in, float* out, int sxi, int syi, int sxo, int syo,
                         const float* lx, const int* ix, const float* ly, const int* iy, cudaStream_t st);
+// Up-sampling into an image with an edge-replicated margin of m pixels on every
+// side; `out` is the start of the (sxo + 2m) x (syo + 2m) buffer, row pitch `pitch`.
+cudaError_t upsample_u8_pad(const uint8_t* in, float* out, int pitch, int m, int sxi, int syi, int sxo, int syo,
+                            const float* lx, const int* ix, const float* ly, const int* iy, cudaStream_t st);
 cudaError_t u8_to_f32(const uint8_t* in, float* out, size_t n, cudaStream_t st);
 
 // Linear image offsets (o1, o2) of every BRIEF sample for one image width, padded
@@ -52,6 +56,12 @@ struct PatternOffsets {
 
 cudaError_t features(const float* up, uint32_t* F, int sx, int sy, int N, int nsp,
                      const int4* pat, int rmax, const PatternOffsets& po, int rev, cudaStream_t st);
+
+// Descriptors from an edge-replicated image: `up` points at pixel (0, 0), row pitch
+// `pitch`, with a margin no narrower than the largest pattern offset; `po` holds the
+// offsets for that pitch.
+cudaError_t features_pad(const float* up, int pitch, uint32_t* F, int sx, int sy, int nsp,
+                         const PatternOffsets& po, int rev, cudaStream_t st);
 
 cudaError_t initialize(const uint32_t* F1, const uint32_t* F2, const uint32_t* flow_prev,
                        uint32_t* flow_out, uint16_t* cost, int sx, int sy, int nsp, int first, int rev,

@@ -66,6 +66,22 @@ __global__ void __launch_bounds__(256) k_upsample(const T* __restrict__ in, floa
     upsample_px<T>(in, out, sxi, syi, sxo, lx, ix, ly, iy, x, y);
 }
 
+// Up-sampling into an edge-replicated image: the output covers (sxo + 2m) x
+// (syo + 2m) pixels at row pitch `pitch`; a pixel of the margin holds the value of
+// the nearest image pixel (each coordinate clamped), computed by the same Lanczos
+// expression, so every read of the margin equals a clamped read of the image.
+template <typename T>
+__global__ void __launch_bounds__(256) k_upsample_pad(const T* __restrict__ in, float* __restrict__ out, int pitch,
+                                                      int m, int sxi, int syi, int sxo, int syo,
+                                                      const float* __restrict__ lx, const int* __restrict__ ix,
+                                                      const float* __restrict__ ly, const int* __restrict__ iy)
+{
+    const int X = blockIdx.x * TX + threadIdx.x, Y = blockIdx.y * TY + threadIdx.y;
+    if (X >= sxo + 2 * m || Y >= syo + 2 * m) return;
+    const int x = min(sxo - 1, max(0, X - m)), y = min(syo - 1, max(0, Y - m));
+    out[X + (size_t)Y * pitch] = upsample_val<T>(in, sxi, syi, lx, ix, ly, iy, x, y);
+}
+
 __global__ void k_u8_to_f32(const uint8_t* __restrict__ in, float* __restrict__ out, size_t n)
 {
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -93,6 +109,25 @@ __global__ void __launch_bounds__(256) k_features(const float* __restrict__ I, u
         if (x >= sx || y >= sy) return;
         features_border_px<NSP>(I, F, sx, sy, N, s_pat, x, y);
     }
+}
+
+// BRIEF descriptors from an edge-replicated image (k_upsample_pad) whose margin is
+// at least the pattern's largest offset: every pixel reads at the linear offsets
+// (no clamping, no border tiles); each thread computes FEAT_PX pixels TX apart.
+constexpr int FEAT_PX = 2;
+template <int NSP>
+__global__ void __launch_bounds__(256) k_features_pad(const float* __restrict__ I, uint32_t* __restrict__ F,
+                                                      int pitch, int sx, int sy,
+                                                      const __grid_constant__ PatternOffsets po, int rev)
+{
+    int bx = blockIdx.x, by = blockIdx.y;
+    if (rev) {
+        bx = gridDim.x - 1 - bx;
+        by = gridDim.y - 1 - by;
+    }
+    const int x = bx * (TX * FEAT_PX) + threadIdx.x, y = by * TY + threadIdx.y;
+    if (x >= sx || y >= sy) return;
+    features_strip_px<NSP, FEAT_PX>(I + (size_t)y * pitch + x, F + ((size_t)y * sx + x) * NSP, sx - x, po.off);
 }
 
 template <int NSP>
@@ -314,6 +349,15 @@ cudaError_t upsample_u8(const uint8_t* in, float* out, int sxi, int syi, int sxo
     return cudaGetLastError();
 }
 
+cudaError_t upsample_u8_pad(const uint8_t* in, float* out, int pitch, int m, int sxi, int syi, int sxo, int syo,
+                            const float* lx, const int* ix, const float* ly, const int* iy, cudaStream_t st)
+{
+    if (m < 0 || pitch < sxo + 2 * m) return cudaErrorInvalidValue;
+    k_upsample_pad<uint8_t><<<grid2d(sxo + 2 * m, syo + 2 * m), dim3(TX, TY), 0, st>>>(in, out, pitch, m, sxi, syi, sxo,
+                                                                                       syo, lx, ix, ly, iy);
+    return cudaGetLastError();
+}
+
 cudaError_t u8_to_f32(const uint8_t* in, float* out, size_t n, cudaStream_t st)
 {
     k_u8_to_f32<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(in, out, n);
@@ -334,6 +378,14 @@ cudaError_t features(const float* up, uint32_t* F, int sx, int sy, int N, int ns
                      const int4* pat, int rmax, const PatternOffsets& po, int rev, cudaStream_t st)
 {
     BM_DISPATCH_NSP(nsp, k_features<NSP><<<grid2d(sx, sy), dim3(TX, TY), 0, st>>>(up, F, sx, sy, N, pat, rmax, po, rev));
+    return cudaGetLastError();
+}
+
+cudaError_t features_pad(const float* up, int pitch, uint32_t* F, int sx, int sy, int nsp,
+                         const PatternOffsets& po, int rev, cudaStream_t st)
+{
+    const dim3 grid((sx + TX * FEAT_PX - 1) / (TX * FEAT_PX), (sy + TY - 1) / TY);
+    BM_DISPATCH_NSP(nsp, k_features_pad<NSP><<<grid, dim3(TX, TY), 0, st>>>(up, F, pitch, sx, sy, po, rev));
     return cudaGetLastError();
 }
 

@@ -88,6 +88,36 @@ def test_features_border_and_interior_paths():
         assert np.array_equal(engine_features(eng, 0), oracle.features(img, pattern, 128))
 
 
+@pytest.mark.parametrize("W,H,u,N", [(90, 60, 2.9, 128), (37, 23, 4.9, 64), (70, 45, 1.5, 512)])
+def test_frame_features_edge_replicated(W, H, u, N):
+    """bm_frame up-samples into an image with an edge-replicated margin and computes
+    the descriptors there with no clamping; they must equal the oracle's clamped
+    descriptors of the same up-sampled image, for the default pattern, a wider one
+    (which re-allocates the margin) and a narrower one.  BM_BUF_UP gives the dense
+    up-sampled image, equal to bm_upsample_u8's."""
+    rng = np.random.default_rng(W)
+    prm = small_params(W, H, u, u, N=N)
+    eng, pattern = make_engine(prm)
+    for k, area in enumerate((None, 4.0 * prm.patchArea, 0.25 * prm.patchArea)):
+        if area is not None:
+            q = small_params(W, H, u, u, N=N)
+            q.patchArea = area
+            pattern = q.make_pattern(20 + k)
+            eng.set_pattern(pattern)
+            eng.reset_sequence()
+        for _ in range(2):
+            u8 = np.clip(np.rint(random_image(rng, W, H)), 0, 255).astype(np.uint8)
+            d8 = _dev(u8)
+            eng.frame(d8.data_ptr(), True)
+            ref = torch.empty(prm.sy, prm.sx, device="cuda")
+            eng.upsample_u8(d8.data_ptr(), ref.data_ptr())
+            eng.synchronize()
+            up = eng.read_buffer(bm.BM_BUF_UP, np.float32, prm.sx * prm.sy).reshape(prm.sy, prm.sx)
+            assert np.array_equal(up, ref.cpu().numpy()), (k, area)
+            # the frame's descriptors are FEAT1 once bm_frame has swapped the slots
+            assert np.array_equal(engine_features(eng, 0), oracle.features(up, pattern, N)), (k, area)
+
+
 def _two_frames(eng, prm, pattern, seed=0):
     rng = np.random.default_rng(seed)
     f1, f2, _, _ = __import__("briefmatch_gb300.synth", fromlist=["make_pair"]).make_pair(seed, prm.sx, prm.sy, 6.0)
