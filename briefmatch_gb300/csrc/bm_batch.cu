@@ -40,7 +40,8 @@ struct PairDev {
     int first_tri_tile_x;  // tiles per row for the trilateral filter (TX x TRI_BY)
     const uint8_t* frame[2];
     float* guide;          // frame 0 as float (the trilateral guide)
-    float* up;
+    float* up;             // up-sampled frame: dense sx*sy, or edge-replicated (below)
+    int up_margin;         // margin the up buffer has room for: (sx+2m)*(sy+2m) floats
     uint32_t* F[2];
     uint32_t* flow[2];
     uint16_t* cost;
@@ -299,6 +300,7 @@ struct bm_batch {
     std::vector<uint32_t> pos;     // caller's pair index -> internal index
     std::vector<size_t> ws;        // working set of each pair (internal order), bytes
     std::vector<PatternOffsets> pattern_off;  // per pair (internal order), for the per-pair descriptor launches
+    std::vector<PatternOffsets> pattern_off_pad;  // the same for the edge-replicated up-sampled image
     int max_fsize = 1, max_tri_s = 0;
     size_t tri_smem = 0;
     int coop_blocks_per_sm = 0, num_sms = 0;
@@ -411,14 +413,24 @@ bm_status enqueue_pair(bm_batch* b, const bm_batch_schedule& s, int j, cudaStrea
     const bool resample = d.sx != d.sx_in || d.sy != d.sy_in;
     BB_CUDA(u8_to_f32(d.frame[0], d.guide, ni, st));
     int rev = 0;
+    // descriptors from the edge-replicated up-sampled image while the pair's pattern
+    // fits the margin its buffer was laid out with; from the dense image otherwise
+    const bool padded = resample && d.rmax <= d.up_margin;
+    const int pitch = d.sx + 2 * d.up_margin;
     for (int which = 0; which < 2; which++) {
-        const float* up = d.up;
-        if (resample) {
-            BB_CUDA(upsample_u8(d.frame[which], d.up, d.sx_in, d.sy_in, d.sx, d.sy, d.lx, d.ix, d.ly, d.iy, st));
+        if (padded) {
+            BB_CUDA(upsample_u8_pad(d.frame[which], d.up, pitch, d.up_margin, d.sx_in, d.sy_in, d.sx, d.sy, d.lx, d.ix,
+                                    d.ly, d.iy, st));
+            BB_CUDA(features_pad(d.up + (size_t)d.up_margin * pitch + d.up_margin, pitch, d.F[which], d.sx, d.sy,
+                                 (int)b->nsp, b->pattern_off_pad[j], rev, st));
         } else {
-            BB_CUDA(u8_to_f32(d.frame[which], d.up, ni, st));
+            if (resample)
+                BB_CUDA(upsample_u8(d.frame[which], d.up, d.sx_in, d.sy_in, d.sx, d.sy, d.lx, d.ix, d.ly, d.iy, st));
+            else
+                BB_CUDA(u8_to_f32(d.frame[which], d.up, ni, st));
+            BB_CUDA(features(d.up, d.F[which], d.sx, d.sy, (int)b->N, (int)b->nsp, d.pat, d.rmax, b->pattern_off[j], rev,
+                             st));
         }
-        BB_CUDA(features(up, d.F[which], d.sx, d.sy, (int)b->N, (int)b->nsp, d.pat, d.rmax, b->pattern_off[j], rev, st));
         rev ^= s.snake ? 1 : 0;
     }
     int cur = 0;
@@ -840,12 +852,24 @@ bm_status bm_batch_create(const bm_params* pairs, uint32_t count, bm_batch** out
     }
     b->flows_bytes = ocur;
     cursor += align256(ocur);
+    // the up-sampled image of a re-sampled pair has room for an edge-replicated margin
+    // as wide as its default pattern's largest offset (per-pair schedule)
+    std::vector<int> margin(count, 0);
+    {
+        std::vector<float> pat(4 * (size_t)b->N);
+        for (uint32_t i = 0; i < count; i++) {
+            const bm_params& p = pairs[i];
+            if (p.sx == p.sx_in && p.sy == p.sy_in) continue;
+            bm_make_pattern(&p, 0, pat.data());
+            for (float v : pat) margin[i] = std::max(margin[i], std::abs((int)v));
+        }
+    }
     for (uint32_t i = 0; i < count; i++) {
         const bm_params& p = pairs[i];
         const size_t n = (size_t)p.sx * p.sy, ni = (size_t)p.sx_in * p.sy_in;
         Off& o = offs[i];
         o.guide = take(ni * 4);
-        o.up = take(n * 4);
+        o.up = take((p.sx + 2 * (size_t)margin[i]) * (p.sy + 2 * (size_t)margin[i]) * 4);
         o.F[0] = take(n * b->nsp * 4);
         o.F[1] = take(n * b->nsp * 4);
         o.flow[0] = take(n * 4);
@@ -923,6 +947,7 @@ bm_status bm_batch_create(const bm_params* pairs, uint32_t count, bm_batch** out
         d.flow_out = reinterpret_cast<float*>(A + b->flows_offset + b->flow_off[i]);
         d.guide = reinterpret_cast<float*>(A + o.guide);
         d.up = reinterpret_cast<float*>(A + o.up);
+        d.up_margin = margin[i];
         d.F[0] = reinterpret_cast<uint32_t*>(A + o.F[0]);
         d.F[1] = reinterpret_cast<uint32_t*>(A + o.F[1]);
         d.flow[0] = reinterpret_cast<uint32_t*>(A + o.flow[0]);
@@ -1031,9 +1056,11 @@ bm_status bm_batch_set_pattern(bm_batch* b, uint32_t pair, const float* h_patter
     if (!b || !h_pattern || pair >= b->count) return bfail(BM_ERR_INVALID, "bm_batch_set_pattern: bad argument");
     if (count != 4 * b->N) return bfail(BM_ERR_INVALID, "bm_batch_set_pattern: expected 4*N values");
     std::vector<int4> pat(b->N);
-    std::vector<int2> off(BM_PATCH_MAX / 4, make_int2(0, 0));
+    std::vector<int2> off(BM_PATCH_MAX / 4, make_int2(0, 0)), off_pad(BM_PATCH_MAX / 4, make_int2(0, 0));
     int rmax = 0;
-    const int sx = b->pairs[b->pos[pair]].sx;
+    const uint32_t j = b->pos[pair];
+    PairDev& d = b->pairs[j];
+    const int sx = d.sx, pitch = d.sx + 2 * d.up_margin;
     for (uint32_t s = 0; s < b->N; s++) {
         int v[4];
         for (int k = 0; k < 4; k++) {
@@ -1042,12 +1069,13 @@ bm_status bm_batch_set_pattern(bm_batch* b, uint32_t pair, const float* h_patter
         }
         pat[s] = make_int4(v[0], v[1], v[2], v[3]);
         off[s] = make_int2(v[0] + v[1] * sx, v[2] + v[3] * sx);
+        off_pad[s] = make_int2(v[0] + v[1] * pitch, v[2] + v[3] * pitch);
     }
-    const uint32_t j = b->pos[pair];
-    PairDev& d = b->pairs[j];
     d.rmax = rmax;
     if (b->pattern_off.size() != b->count) b->pattern_off.resize(b->count);
+    if (b->pattern_off_pad.size() != b->count) b->pattern_off_pad.resize(b->count);
     std::memcpy(b->pattern_off[j].off, off.data(), sizeof(b->pattern_off[j].off));
+    std::memcpy(b->pattern_off_pad[j].off, off_pad.data(), sizeof(b->pattern_off_pad[j].off));
     BB_CUDA(cudaMemcpyAsync((void*)d.pat, pat.data(), b->N * sizeof(int4), cudaMemcpyHostToDevice, b->stream));
     BB_CUDA(cudaMemcpyAsync((void*)d.off, off.data(), off.size() * sizeof(int2), cudaMemcpyHostToDevice, b->stream));
     if (b->d_pairs)

@@ -113,8 +113,11 @@ __global__ void __launch_bounds__(256) k_features(const float* __restrict__ I, u
 
 // BRIEF descriptors from an edge-replicated image (k_upsample_pad) whose margin is
 // at least the pattern's largest offset: every pixel reads at the linear offsets
-// (no clamping, no border tiles); each thread computes FEAT_PX pixels TX apart.
-constexpr int FEAT_PX = 2;
+// (no clamping, no border tiles); each thread computes feat_px<NSP>() pixels TX apart
+// (two up to 128-bit descriptors, where sharing each offset's address arithmetic
+// pays; one for longer ones, whose descriptor words would cost occupancy).
+template <int NSP>
+__host__ __device__ constexpr int feat_px() { return NSP <= 4 ? 2 : 1; }
 template <int NSP>
 __global__ void __launch_bounds__(256) k_features_pad(const float* __restrict__ I, uint32_t* __restrict__ F,
                                                       int pitch, int sx, int sy,
@@ -125,9 +128,9 @@ __global__ void __launch_bounds__(256) k_features_pad(const float* __restrict__ 
         bx = gridDim.x - 1 - bx;
         by = gridDim.y - 1 - by;
     }
-    const int x = bx * (TX * FEAT_PX) + threadIdx.x, y = by * TY + threadIdx.y;
+    const int x = bx * (TX * feat_px<NSP>()) + threadIdx.x, y = by * TY + threadIdx.y;
     if (x >= sx || y >= sy) return;
-    features_strip_px<NSP, FEAT_PX>(I + (size_t)y * pitch + x, F + ((size_t)y * sx + x) * NSP, sx - x, po.off);
+    features_strip_px<NSP, feat_px<NSP>()>(I + (size_t)y * pitch + x, F + ((size_t)y * sx + x) * NSP, sx - x, po.off);
 }
 
 template <int NSP>
@@ -384,8 +387,11 @@ cudaError_t features(const float* up, uint32_t* F, int sx, int sy, int N, int ns
 cudaError_t features_pad(const float* up, int pitch, uint32_t* F, int sx, int sy, int nsp,
                          const PatternOffsets& po, int rev, cudaStream_t st)
 {
-    const dim3 grid((sx + TX * FEAT_PX - 1) / (TX * FEAT_PX), (sy + TY - 1) / TY);
-    BM_DISPATCH_NSP(nsp, k_features_pad<NSP><<<grid, dim3(TX, TY), 0, st>>>(up, F, pitch, sx, sy, po, rev));
+    BM_DISPATCH_NSP(nsp, {
+        const int w = TX * feat_px<NSP>();
+        k_features_pad<NSP><<<dim3((sx + w - 1) / w, (sy + TY - 1) / TY), dim3(TX, TY), 0, st>>>(up, F, pitch, sx, sy,
+                                                                                                 po, rev);
+    });
     return cudaGetLastError();
 }
 

@@ -64,6 +64,37 @@ def test_batch_equals_single_pairs(sched):
     b.close()
 
 
+@pytest.mark.parametrize("per_pair", [0, 1])
+def test_batch_patterns_wider_and_narrower_than_margin(per_pair):
+    """The per-pair schedule takes descriptors from an edge-replicated up-sampled image
+    whose margin is sized for each pair's default pattern; a wider pattern set later
+    falls back to the clamped descriptors.  Both equal single contexts with the same
+    patterns."""
+    params, frames = _batch_inputs()
+    patterns = []
+    for k, p in enumerate(params):
+        q = bm.BMParams.derive(p.sx_in, p.sy_in, 2.0, 2.0, N=64)
+        q.patchArea = p.patchArea * (4.0 if k % 2 == 0 else 0.25)
+        patterns.append(q.make_pattern(50 + k))
+    want = []
+    for p, pat, (f0, f1) in zip(params, patterns, frames):
+        eng = bm.FlowEngine(p)
+        eng.set_pattern(pat)
+        eng.process_frame(f0)
+        want.append(eng.process_frame(f1))
+        eng.clean()
+    b = bm.Batch(params)
+    for k, pat in enumerate(patterns):
+        b.set_pattern(k, pat)
+    b.set_schedule(per_pair=per_pair, persistent=0, snake=1, use_graph=1)
+    b.load_frames(b.pack_frames(frames))
+    b.run()
+    b.synchronize()
+    for k, ((gu, gv), (wu, wv)) in enumerate(zip(b.read_flows(), want)):
+        assert np.array_equal(gu, wu) and np.array_equal(gv, wv), k
+    b.close()
+
+
 def test_batch_n128_and_unfiltered():
     params = [bm.BMParams.derive(w, h, 1.5, 1.5, N=128, filter=0) for w, h in SIZES[:3]]
     frames = [synth.make_pair(40 + k, w, h, 4.0)[:2] for k, (w, h) in enumerate(SIZES[:3])]
