@@ -179,14 +179,25 @@ def measured_peaks():
 
 
 def ncu_traffic(kernel):
-    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any.  The
+    file's `workload W H up N` line names the workload it was captured on; other
+    workloads get None (their working sets sit differently against L2, so the
+    traffic does not scale with the pixel count)."""
     path = os.path.join(ROOT, "profiles", "traffic_per_launch.txt")
     if not os.path.exists(path):
         return None
     with open(path) as f:
-        for line in f:
-            parts = line.split()
-            if len(parts) >= 2 and parts[0] == kernel:
+        lines = [ln.split() for ln in f if ln.strip()]
+    for parts in lines:
+        if parts[0] == "workload":
+            try:
+                w, h, up, n = int(parts[1]), int(parts[2]), float(parts[3]), int(parts[4])
+            except (IndexError, ValueError):
+                return None
+            if (w, h, up, n) != (W, H, UP, NBITS):
+                return None
+    for parts in lines:
+        if len(parts) >= 2 and parts[0] == kernel:
                 try:
                     return float(parts[1])
                 except ValueError:
