@@ -5,6 +5,7 @@
 #pragma once
 
 #include <curand_kernel.h>
+#include <type_traits>
 
 #include "bm_internal.h"
 
@@ -162,7 +163,7 @@ __device__ __forceinline__ f2x ex2_2(f2x a) { return pk2(exp2f(lo2(a)), exp2f(hi
 // accumulation runs in the reference's order (i outer, j inner).
 // ---------------------------------------------------------------------------
 template <typename T>
-__device__ __forceinline__ float upsample_val(const T* __restrict__ in, int sxi, int syi,
+__device__ __forceinline__ float upsample_val(const T* __restrict__ in, int sxi, int syi, int sxo, int syo,
                                               const float* __restrict__ lx, const int* __restrict__ ix,
                                               const float* __restrict__ ly, const int* __restrict__ iy, int x, int y)
 {
@@ -171,13 +172,13 @@ __device__ __forceinline__ float upsample_val(const T* __restrict__ in, int sxi,
     int row[6];
 #pragma unroll
     for (int b = 0; b < 6; b++) {
-        Ly[b] = ly[y * 6 + b];
+        Ly[b] = ly[b * syo + y];
         row[b] = min(syi - 1, max(0, y1 - 2 + b)) * sxi;
     }
     float v = 0.0f, w = 0.0f;
 #pragma unroll
     for (int a = 0; a < 6; a++) {
-        float Lx = lx[x * 6 + a];
+        float Lx = lx[a * sxo + x];
         int ci = min(sxi - 1, max(0, x1 - 2 + a));
 #pragma unroll
         for (int b = 0; b < 6; b++) {
@@ -190,10 +191,10 @@ __device__ __forceinline__ float upsample_val(const T* __restrict__ in, int sxi,
 
 template <typename T>
 __device__ __forceinline__ void upsample_px(const T* __restrict__ in, float* __restrict__ out, int sxi, int syi,
-                                            int sxo, const float* __restrict__ lx, const int* __restrict__ ix,
+                                            int sxo, int syo, const float* __restrict__ lx, const int* __restrict__ ix,
                                             const float* __restrict__ ly, const int* __restrict__ iy, int x, int y)
 {
-    out[x + (size_t)y * sxo] = upsample_val<T>(in, sxi, syi, lx, ix, ly, iy, x, y);
+    out[x + (size_t)y * sxo] = upsample_val<T>(in, sxi, syi, sxo, syo, lx, ix, ly, iy, x, y);
 }
 
 // ---------------------------------------------------------------------------
@@ -679,27 +680,40 @@ __device__ __forceinline__ void trilateral_block(const float* __restrict__ U, co
         const float2* col = suv + row0 * TW + threadIdx.x + s + i;
         const float* colI = sI + row0 * TW + threadIdx.x + s + i;
         f2x cuA = 0, cuB = 0, cvA = 0, cvB = 0, cwA = 0, cwB = 0;
-#pragma unroll 4
-        for (int m = 0; m < NR; m++) {
+        // source row m lies in output r's window when 0 <= m - r < 2s: pair A (outputs
+        // 0, 1) has none of its rows past m = 2s, pair B (outputs 2, 3) none before
+        // m = 2; those evaluations would add exact zeros and are skipped
+        auto tap = [&](int m, auto doA, auto doB) {
             const float2 uv = col[m * TW];
             const float i1 = colI[m * TW];
             const float4 rf = rowf[m];
             const f2x uu = pk2(uv.x, uv.x), vv = pk2(uv.y, uv.y), ii = pk2(i1, i1);
-            f2x du = fma2(uu, kEE, umA), dv = fma2(vv, kEE, vmA), dI = fma2(ii, kII, IA);
-            f2x q = fma2(dI, dI, fma2(dv, dv, fma2(du, du, pk2(rf.x, rf.y))));
-            f2x w = ex2n_2(mul2(q, rr));
-            cuA = fma2(w, uu, cuA);
-            cvA = fma2(w, vv, cvA);
-            cwA = add2(cwA, w);
-            du = fma2(uu, kEE, umB);
-            dv = fma2(vv, kEE, vmB);
-            dI = fma2(ii, kII, IB);
-            q = fma2(dI, dI, fma2(dv, dv, fma2(du, du, pk2(rf.z, rf.w))));
-            w = ex2n_2(mul2(q, rr));
-            cuB = fma2(w, uu, cuB);
-            cvB = fma2(w, vv, cvB);
-            cwB = add2(cwB, w);
-        }
+            if constexpr (decltype(doA)::value) {
+                const f2x du = fma2(uu, kEE, umA), dv = fma2(vv, kEE, vmA), dI = fma2(ii, kII, IA);
+                const f2x q = fma2(dI, dI, fma2(dv, dv, fma2(du, du, pk2(rf.x, rf.y))));
+                const f2x w = ex2n_2(mul2(q, rr));
+                cuA = fma2(w, uu, cuA);
+                cvA = fma2(w, vv, cvA);
+                cwA = add2(cwA, w);
+            }
+            if constexpr (decltype(doB)::value) {
+                const f2x du = fma2(uu, kEE, umB), dv = fma2(vv, kEE, vmB), dI = fma2(ii, kII, IB);
+                const f2x q = fma2(dI, dI, fma2(dv, dv, fma2(du, du, pk2(rf.z, rf.w))));
+                const f2x w = ex2n_2(mul2(q, rr));
+                cuB = fma2(w, uu, cuB);
+                cvB = fma2(w, vv, cvB);
+                cwB = add2(cwB, w);
+            }
+        };
+        static_assert(TRI_R == 4, "the row split below assumes two output pairs");
+        using yes = std::true_type;
+        using no = std::false_type;
+        tap(0, yes{}, no{});
+        tap(1, yes{}, no{});
+#pragma unroll 4
+        for (int m = 2; m <= 2 * s; m++) tap(m, yes{}, yes{});
+        tap(2 * s + 1, no{}, yes{});
+        tap(2 * s + 2, no{}, yes{});
         const float wi = exp2f(-(float)(i * i) * cS);
         const f2x wi2 = pk2(wi, wi);
         ufA = fma2(wi2, cuA, ufA);
