@@ -554,44 +554,52 @@ __device__ __forceinline__ void downsample_px(const uint32_t* __restrict__ flow,
 }
 
 // ---------------------------------------------------------------------------
-// 1-D median (util_cuda.cu:75-111) at (x, y): linear-index window of fsize samples,
-// guard 0 outside the plane, held in registers padded with +inf up to FS; the first
-// ks+1 positions are sorted as in the reference and v[ks] is the median.
+// 1-D median (util_cuda.cu:75-111) of the two outputs at linear indices p and
+// p + step (the second only when `second`): each window is fsize samples at linear
+// offsets -ks .. fsize-1-ks (ks = fsize/2), guard 0 outside the plane, and the median
+// is the (ks+1)-th smallest.  The two windows share the fsize-1 samples S between
+// them; with a the first output's own sample and b the second's, the (ks+1)-th
+// smallest of S + {a} is min(max(a, S(ks-1)), S(ks)), S(i) the (i+1)-th smallest of
+// S, so one partial selection (positions 0..ks, in registers padded with +inf up to
+// FS-1) serves both outputs.
 // ---------------------------------------------------------------------------
 template <int FS>
-__device__ __forceinline__ void median_px(const float* __restrict__ in, float* __restrict__ out, int dir, int fsize,
-                                          int sx, int sy, int x, int y)
+__device__ __forceinline__ void median2_px(const float* __restrict__ in, float* __restrict__ out, long p, long step,
+                                           long n, int fsize, bool second)
 {
-    const long n = (long)sx * sy;
-    const long base = x + (long)y * sx;
-    const long step = dir ? 1 : sx;
     const int ks = fsize / 2;
-    float v[FS];
-#pragma unroll
-    for (int k = 0; k < FS; k++) {
-        if (k < fsize) {
-            const long idx = base + (long)(k - ks) * step;
-            v[k] = (idx >= 0 && idx < n) ? __ldg(in + idx) : 0.0f;
-        } else {
-            v[k] = __int_as_float(0x7f800000);
-        }
+    auto sample = [&](long idx) { return (idx >= 0 && idx < n) ? __ldg(in + idx) : 0.0f; };
+    const float a = sample(p - (long)ks * step);
+    const float b = second ? sample(p + (long)(fsize - ks) * step) : 0.0f;
+    if (fsize == 1) {
+        out[p] = a;
+        if (second) out[p + step] = b;
+        return;
     }
+    float v[FS - 1];
+#pragma unroll
+    for (int k = 0; k < FS - 1; k++)
+        v[k] = (k < fsize - 1) ? sample(p + (long)(k - ks + 1) * step) : __int_as_float(0x7f800000);
 #pragma unroll
     for (int i = 0; i < (FS + 1) / 2; i++) {
         if (i <= ks) {
 #pragma unroll
-            for (int j = i + 1; j < FS; j++) {
-                const float a = v[i], b = v[j];
-                v[i] = fminf(a, b);
-                v[j] = fmaxf(a, b);
+            for (int j = i + 1; j < FS - 1; j++) {
+                const float x = v[i], y = v[j];
+                v[i] = fminf(x, y);
+                v[j] = fmaxf(x, y);
             }
         }
     }
-    float r = v[0];
+    float lo = v[0], hi = v[1];
 #pragma unroll
     for (int i = 1; i < (FS + 1) / 2; i++)
-        if (i == ks) r = v[i];
-    out[base] = r;
+        if (i == ks) {
+            lo = v[i - 1];
+            hi = v[i];
+        }
+    out[p] = fminf(fmaxf(a, lo), hi);
+    if (second) out[p + step] = fminf(fmaxf(b, lo), hi);
 }
 
 // ---------------------------------------------------------------------------

@@ -250,15 +250,29 @@ __global__ void k_flow_to_planes(const uint32_t* __restrict__ flow, float* __res
 }
 
 
-// Separable 1-D median, both components in one launch (blockIdx.z).
+// Separable 1-D median, both components in one launch (blockIdx.z).  Each thread
+// computes two outputs adjacent along the filter direction (median2_px): down a
+// column (dir 0) the rows y and y+1; along the rows (dir 1) the linear indices 2t and
+// 2t+1 (the reference's window runs over linear indices, so a pair may span a row
+// end).
 template <int FS>
 __global__ void __launch_bounds__(256) k_median_pass(const float* __restrict__ inU, const float* __restrict__ inV,
                                                      float* __restrict__ outU, float* __restrict__ outV,
                                                      int dir, int fsize, int sx, int sy)
 {
-    const int x = blockIdx.x * TX + threadIdx.x, y = blockIdx.y * TY + threadIdx.y;
-    if (x >= sx || y >= sy) return;
-    median_px<FS>(blockIdx.z ? inV : inU, blockIdx.z ? outV : outU, dir, fsize, sx, sy, x, y);
+    static_assert(FS % 2 == 1, "median register windows are odd");
+    const float* in = blockIdx.z ? inV : inU;
+    float* out = blockIdx.z ? outV : outU;
+    const long n = (long)sx * sy;
+    if (dir) {
+        const long p = 2 * ((long)blockIdx.x * (TX * TY) + threadIdx.y * TX + threadIdx.x);
+        if (p >= n) return;
+        median2_px<FS>(in, out, p, 1, n, fsize, p + 1 < n);
+    } else {
+        const int x = blockIdx.x * TX + threadIdx.x, y = 2 * (blockIdx.y * TY + threadIdx.y);
+        if (x >= sx || y >= sy) return;
+        median2_px<FS>(in, out, x + (long)y * sx, sx, n, fsize, y + 1 < sy);
+    }
 }
 
 __global__ void __launch_bounds__(TX * TRI_TY) k_trilateral_x2(const float* __restrict__ U, const float* __restrict__ V,
@@ -471,8 +485,9 @@ cudaError_t flow_to_planes(const uint32_t* flow, float* U, float* V, size_t n, c
 cudaError_t median_pass(const float* inU, const float* inV, float* outU, float* outV,
                         int dir, int fsize, int sx, int sy, cudaStream_t st)
 {
-    dim3 g = grid2d(sx, sy);
-    g.z = 2;
+    const long n = (long)sx * sy;
+    const dim3 g = dir ? dim3((unsigned)((n + 2 * TX * TY - 1) / (2 * TX * TY)), 1, 2)
+                       : dim3((sx + TX - 1) / TX, (sy + 2 * TY - 1) / (2 * TY), 2);
 #define BM_MED(FSV) k_median_pass<FSV><<<g, dim3(TX, TY), 0, st>>>(inU, inV, outU, outV, dir, fsize, sx, sy)
     if (fsize <= 9) BM_MED(9);
     else if (fsize <= 13) BM_MED(13);

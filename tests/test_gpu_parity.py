@@ -210,7 +210,7 @@ def test_downsample_bit_exact(W, H, u):
     assert np.abs(nn[0].astype(np.int64) - ieee).max() <= 1
 
 
-@pytest.mark.parametrize("fsize", [1, 3, 9, 13, 15, 23, 31, 47])
+@pytest.mark.parametrize("fsize", [1, 2, 3, 9, 12, 13, 15, 23, 30, 31, 46, 47])
 def test_median_and_trilateral(fsize):
     W, H = 97, 61
     prm = small_params(W, H, 1.5, 1.5, N=32)
