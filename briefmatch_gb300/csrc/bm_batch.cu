@@ -154,7 +154,7 @@ __global__ void __launch_bounds__(256) k_b_upsample(BatchDev bd, int which)
     if (P.sx == P.sx_in && P.sy == P.sy_in)
         P.up[(size_t)y * P.sx + x] = (float)P.frame[which][(size_t)y * P.sx + x];
     else
-        upsample_px<uint8_t>(P.frame[which], P.up, P.sx_in, P.sy_in, P.sx, P.sy, P.lx, P.ix, P.ly, P.iy, x, y);
+        upsample_px<uint8_t>(P.frame[which], P.up, P.sx_in, P.sy_in, P.sx, P.lx, P.ix, P.ly, P.iy, x, y);
 }
 
 // Tile `tile` of the up-sampled grids, visited in reverse order when rev is set.

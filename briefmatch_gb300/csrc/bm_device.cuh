@@ -163,7 +163,7 @@ __device__ __forceinline__ f2x ex2_2(f2x a) { return pk2(exp2f(lo2(a)), exp2f(hi
 // accumulation runs in the reference's order (i outer, j inner).
 // ---------------------------------------------------------------------------
 template <typename T>
-__device__ __forceinline__ float upsample_val(const T* __restrict__ in, int sxi, int syi, int sxo, int syo,
+__device__ __forceinline__ float upsample_val(const T* __restrict__ in, int sxi, int syi,
                                               const float* __restrict__ lx, const int* __restrict__ ix,
                                               const float* __restrict__ ly, const int* __restrict__ iy, int x, int y)
 {
@@ -172,13 +172,13 @@ __device__ __forceinline__ float upsample_val(const T* __restrict__ in, int sxi,
     int row[6];
 #pragma unroll
     for (int b = 0; b < 6; b++) {
-        Ly[b] = ly[b * syo + y];
+        Ly[b] = ly[y * 6 + b];
         row[b] = min(syi - 1, max(0, y1 - 2 + b)) * sxi;
     }
     float v = 0.0f, w = 0.0f;
 #pragma unroll
     for (int a = 0; a < 6; a++) {
-        float Lx = lx[a * sxo + x];
+        float Lx = lx[x * 6 + a];
         int ci = min(sxi - 1, max(0, x1 - 2 + a));
 #pragma unroll
         for (int b = 0; b < 6; b++) {
@@ -191,10 +191,10 @@ __device__ __forceinline__ float upsample_val(const T* __restrict__ in, int sxi,
 
 template <typename T>
 __device__ __forceinline__ void upsample_px(const T* __restrict__ in, float* __restrict__ out, int sxi, int syi,
-                                            int sxo, int syo, const float* __restrict__ lx, const int* __restrict__ ix,
+                                            int sxo, const float* __restrict__ lx, const int* __restrict__ ix,
                                             const float* __restrict__ ly, const int* __restrict__ iy, int x, int y)
 {
-    out[x + (size_t)y * sxo] = upsample_val<T>(in, sxi, syi, sxo, syo, lx, ix, ly, iy, x, y);
+    out[x + (size_t)y * sxo] = upsample_val<T>(in, sxi, syi, lx, ix, ly, iy, x, y);
 }
 
 // ---------------------------------------------------------------------------

@@ -36,9 +36,7 @@ __device__ __forceinline__ int2 block_tile(int rev)
 }
 
 // Lanczos weight tables (util_cuda.cu:134-151): per output column (or row) the six
-// weights with the reference's expression, stored tap-major (w[k*n_out + x], so the
-// lanes of a warp read one tap's weights of consecutive columns together), and the
-// first tap index.
+// weights with the reference's expression and the first tap index.
 __global__ void k_lanczos_tables(float* __restrict__ w, int* __restrict__ idx, int n_in, int n_out)
 {
     int x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -51,7 +49,7 @@ __global__ void k_lanczos_tables(float* __restrict__ w, int* __restrict__ idx, i
         float xx = BM_PI * (xp - i);
         float L = a * sin(xx) * sin(xx / a) / (xx * xx);
         if (L != L) L = 1;
-        w[k * n_out + x] = L;
+        w[x * 6 + k] = L;
     }
     idx[x] = x1;
 }
@@ -65,7 +63,7 @@ __global__ void __launch_bounds__(256) k_upsample(const T* __restrict__ in, floa
 {
     const int x = blockIdx.x * TX + threadIdx.x, y = blockIdx.y * TY + threadIdx.y;
     if (x >= sxo || y >= syo) return;
-    upsample_px<T>(in, out, sxi, syi, sxo, syo, lx, ix, ly, iy, x, y);
+    upsample_px<T>(in, out, sxi, syi, sxo, lx, ix, ly, iy, x, y);
 }
 
 // Up-sampling into an edge-replicated image: the output covers (sxo + 2m) x
@@ -81,7 +79,7 @@ __global__ void __launch_bounds__(256) k_upsample_pad(const T* __restrict__ in, 
     const int X = blockIdx.x * TX + threadIdx.x, Y = blockIdx.y * TY + threadIdx.y;
     if (X >= sxo + 2 * m || Y >= syo + 2 * m) return;
     const int x = min(sxo - 1, max(0, X - m)), y = min(syo - 1, max(0, Y - m));
-    out[X + (size_t)Y * pitch] = upsample_val<T>(in, sxi, syi, sxo, syo, lx, ix, ly, iy, x, y);
+    out[X + (size_t)Y * pitch] = upsample_val<T>(in, sxi, syi, lx, ix, ly, iy, x, y);
 }
 
 __global__ void k_u8_to_f32(const uint8_t* __restrict__ in, float* __restrict__ out, size_t n)
