@@ -403,17 +403,21 @@ bm_status set_pattern_impl(bm_ctx* c, const float* h_pattern)
     }
     // the working up-sampled image's margin must cover the largest offset
     const bm_params& p = c->prm;
+    // (the new image is allocated first: if that fails, the previous pattern and
+    // working image stay in effect)
     if ((p.sx != p.sx_in || p.sy != p.sy_in) && (!c->d_upad || rmax > c->up_margin)) {
-        BM_CUDA(cudaStreamSynchronize(c->stream));
-        if (c->d_upad) BM_CUDA(cudaFree(c->d_upad));
-        c->d_upad = nullptr;
-        c->upad_valid = false;
-        c->up_margin = rmax;
-        const bm_status st = dev_alloc(&c->d_upad, (size_t)c->up_pitch() * (p.sy + 2 * (size_t)rmax));
-        if (st != BM_OK) {
-            c->up_margin = 0;
-            return st;
+        float* fresh = nullptr;
+        const bm_status st = dev_alloc(&fresh, (p.sx + 2 * (size_t)rmax) * (p.sy + 2 * (size_t)rmax));
+        if (st != BM_OK) return st;
+        const cudaError_t e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) {
+            cudaFree(fresh);
+            return fail(BM_ERR_CUDA, "bm_set_pattern: %s", cudaGetErrorString(e));
         }
+        if (c->d_upad) cudaFree(c->d_upad);
+        c->d_upad = fresh;
+        c->up_margin = rmax;
+        c->upad_valid = false;
     }
     std::memset(&c->pattern_off, 0, sizeof(c->pattern_off));
     std::memset(&c->pattern_off_pad, 0, sizeof(c->pattern_off_pad));
