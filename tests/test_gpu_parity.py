@@ -92,13 +92,13 @@ def test_features_border_and_interior_paths():
 def test_frame_features_edge_replicated(W, H, u, N):
     """bm_frame up-samples into an image with an edge-replicated margin and computes
     the descriptors there with no clamping; they must equal the oracle's clamped
-    descriptors of the same up-sampled image, for the default pattern, a wider one
-    (which re-allocates the margin) and a narrower one.  BM_BUF_UP gives the dense
-    up-sampled image, equal to bm_upsample_u8's."""
+    descriptors of the same up-sampled image, for the default pattern, wider ones
+    (which re-allocate the margin) and a narrower one.  BM_BUF_UP gives the dense up-sampled image, equal to
+    bm_upsample_u8's."""
     rng = np.random.default_rng(W)
     prm = small_params(W, H, u, u, N=N)
     eng, pattern = make_engine(prm)
-    for k, area in enumerate((None, 4.0 * prm.patchArea, 0.25 * prm.patchArea)):
+    for k, area in enumerate((None, 4.0 * prm.patchArea, 16.0 * prm.patchArea, 0.25 * prm.patchArea)):
         if area is not None:
             q = small_params(W, H, u, u, N=N)
             q.patchArea = area
