@@ -124,7 +124,10 @@ bm_status bm_synchronize(bm_ctx* ctx);
 /* CUDA_copyPatchToConst, briefmatch_cuda.cu:376-379: install 4*N pattern values. */
 bm_status bm_set_pattern(bm_ctx* ctx, const float* h_pattern, uint32_t count);
 
-/* Pointer and byte size of one of the context's device buffers. */
+/* Pointer and byte size of one of the context's device buffers.  Their contents are
+ * valid once the work queued on the context's stream is done.  BM_BUF_UP is a dense
+ * sx*sy copy of the engine's working up-sampled image (which carries an
+ * edge-replicated margin); bm_buffer queues that copy on the context's stream. */
 bm_status bm_buffer(bm_ctx* ctx, bm_buffer_id id, void** d_ptr, size_t* bytes);
 
 /* Copy bytes between a context buffer and caller memory (host or device memory
