@@ -56,12 +56,9 @@ SEED = 20261203
 
 
 def set_config(name):
-    global W, H, FRAMES, UP, NBITS, VMAX, PAIRS, WORKLOAD
+    global W, H, FRAMES, UP, NBITS, VMAX, PAIRS
     W, H, FRAMES, UP, NBITS, VMAX = CONFIGS[name]
     PAIRS = FRAMES - 1
-    WORKLOAD = ("%%s engine, synthetic %dx%d 8-bit sequence of %d frames (%d pair%s, |v|<=%g px), "
-                "up-sampling %gx%g, feature_length %d, temporal init, FP32 flow out"
-                % (W, H, FRAMES, PAIRS, "s" if PAIRS > 1 else "", VMAX, UP, UP, NBITS))
 
 
 set_config("2")
@@ -205,10 +202,34 @@ def ncu_traffic(kernel):
     return None
 
 
-def make_workload(rank):
-    from briefmatch_gb300 import synth
+def synth_module():
+    """The seeded synthetic generator (briefmatch_gb300/synth.py, numpy and scipy
+    only), loaded from its file so that the reference arm does not import the engine
+    package."""
+    import importlib.util
 
-    return synth.make_sequence(SEED + rank, W, H, FRAMES, vmax=VMAX)
+    mod = sys.modules.get("bm_bench_synth")
+    if mod is None:
+        spec = importlib.util.spec_from_file_location("bm_bench_synth", os.path.join(ROOT, "briefmatch_gb300",
+                                                                                     "synth.py"))
+        mod = importlib.util.module_from_spec(spec)
+        sys.modules["bm_bench_synth"] = mod
+        spec.loader.exec_module(mod)
+    return mod
+
+
+def make_workload(rank):
+    return synth_module().make_sequence(SEED + rank, W, H, FRAMES, vmax=VMAX)
+
+
+def bench_config(world):
+    """The workload both arms report (identical in the engine and reference lines)."""
+    return {"workload": "synthetic %dx%d 8-bit sequence of %d frames (%d pair%s, |v|<=%g px), up-sampling %gx%g, "
+                        "feature_length %d, temporal init, FP32 flow out"
+                        % (W, H, FRAMES, PAIRS, "s" if PAIRS > 1 else "", VMAX, UP, UP, NBITS),
+            "width": W, "height": H, "frames_per_step": FRAMES, "pairs_per_step": PAIRS, "upsampling": UP,
+            "feature_length": NBITS, "l2": "flushed (256 MB write) before every timed step",
+            "parallelism": "replicas" if world > 1 else "single GPU"}
 
 
 def algorithmic_bytes(kernel, prm):
@@ -410,9 +431,7 @@ def choose_schedule(torch, prm, pattern, net, stream):
     engine's there.  Returns (schedule or None, table)."""
     import numpy as np
 
-    from briefmatch_gb300 import synth
-
-    frames, flows = synth.make_sequence(SEED + 7777, W, H, FRAMES, vmax=VMAX)
+    frames, flows = synth_module().make_sequence(SEED + 7777, W, H, FRAMES, vmax=VMAX)
     d = torch.from_numpy(np.stack(frames)).cuda()
     fp = [d[k].data_ptr() for k in range(FRAMES)]
     u = torch.empty(PAIRS, H, W, device="cuda")
@@ -546,36 +565,56 @@ def run_engine(args, torch, world, rank):
         cpu = cpu_baseline(prm, pattern, frames, args.cpu_pairs)
 
     sched = learned["schedule"] if head_name != "plain" else {"iterations": prm.iterations, "jfMax": prm.jfMax}
+    # the reference's own kernels (compiled from its sources) over the same step on this GPU
+    ref_cuda = None
+    if rank == 0 and world == 1:
+        try:
+            ref_cuda = reference_cuda(torch, prm.as_dict(), pattern, prm.gauss_taps(), frames, args)
+        except Exception as e:  # the reference kernel build is optional
+            ref_cuda = {"unavailable": str(e)[:200]}
+    vs_ref = None
+    if ref_cuda and ref_cuda.get("value"):
+        rv = ref_cuda["value"]
+        vs_ref = {"headline": head["value"] / rv, "plain": rp["value"] / rv, "e2e": e2e["value"] / rv,
+                  "reference_mpx_s": rv}
+        if learned and learned.get("value"):
+            vs_ref["learned"] = learned["value"] / rv
+    # long strings (autotune reports) go to stderr so the line's head stays short
+    if batched:
+        for key, rep in (("batched", batched.get("autotune")),
+                         ("batched learned", (batched.get("learned") or {}).get("autotune"))):
+            if rep:
+                print("autotune %s: %s" % (key, rep), file=sys.stderr, flush=True)
+        batched.pop("autotune", None)
+        if batched.get("learned"):
+            batched["learned"].pop("autotune", None)
     line = {
         "metric": METRIC, "value": head["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u32 descriptors / int16 field / f32 flow",
         "data": "synthetic (seeded generator; see bench.py)",
-        "config": {"workload": WORKLOAD % head_name, "engine": head_name, "width": W, "height": H,
-                   "frames_per_step": FRAMES, "pairs_per_step": PAIRS, "upsampling": UP, "feature_length": NBITS,
-                   "grid": [prm.sx, prm.sy], "iterations": sched["iterations"], "jfMax": sched["jfMax"],
-                   "local_steps": sched.get("local_steps", 0),
-                   "fsize": prm.fsize, "l2": "flushed (256 MB write) before every timed step",
-                   "pipelined": PIPELINED,
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
-        "epe": {"mean": float(np.mean(head["epe"])), "per_pair": [round(e, 4) for e in head["epe"]],
-                "plain_mean": float(np.mean(rp["epe"]))},
+        "config": bench_config(world),
+        "engine": {"name": head_name, "iterations": sched["iterations"], "jfMax": sched["jfMax"],
+                   "local_steps": sched.get("local_steps", 0), "grid": [prm.sx, prm.sy], "fsize": prm.fsize,
+                   "pipelined": PIPELINED},
         "plain": {"value": rp["value"], "ms_per_step": rp["ms_per_step"], "epe_mean": float(np.mean(rp["epe"])),
                   "gpu_launches": int(rp["launches"]), "iterations": prm.iterations, "jfMax": prm.jfMax},
-        "learned": learned,
+        "learned_vs_plain": (learned["speedup_vs_plain"] if learned and learned.get("value") else None),
+        "batched_learned_vs_plain_batch": ((batched.get("learned") or {}).get("speedup_vs_plain_batch")
+                                           if batched else None),
+        "vs_reference_cuda_build": vs_ref,
         "e2e": e2e,
         "gpu_launches": int(head["launches"]),
         "clocks": head["clocks"],
         "roofline": roofline,
-        "kernels": kernels,
         "cpu_baseline": cpu,
+        "epe": {"mean": float(np.mean(head["epe"])), "per_pair": [round(e, 4) for e in head["epe"]],
+                "plain_mean": float(np.mean(rp["epe"]))},
+        "reference_cuda_build": ref_cuda,
+        "learned": learned,
+        "kernels": kernels,
         "batched": batched,
     }
-    if args.config != "2" and rank == 0 and world == 1:
-        try:
-            line["reference_cuda_build"] = reference_cuda(torch, prm, pattern, frames, args)
-        except Exception as e:  # the reference kernel build is optional
-            line["reference_cuda_build"] = {"unavailable": str(e)[:200]}
     if rank == 0:
         print(json.dumps(line), flush=True)
     plain.clean()
@@ -590,9 +629,7 @@ BATCH_SEED = 20261204
 
 def _make_batch_pair(args):
     seed, w, h = args
-    from briefmatch_gb300 import synth
-
-    f0, f1, u, v = synth.make_pair(seed, w, h, vmax=15.0)
+    f0, f1, u, v = synth_module().make_pair(seed, w, h, vmax=15.0)
     return f0, f1, u, v
 
 
@@ -602,10 +639,8 @@ def make_batch_workload(pairs, seed=None):
     spawn-started process pool."""
     import multiprocessing as mp
 
-    from briefmatch_gb300 import synth
-
     seed = BATCH_SEED if seed is None else seed
-    sizes = synth.make_batch_sizes(seed, count=pairs)
+    sizes = synth_module().make_batch_sizes(seed, count=pairs)
     jobs = [(seed + k, w, h) for k, (w, h) in enumerate(sizes)]
     with mp.get_context("spawn").Pool(min(16, os.cpu_count() or 1)) as pool:
         data = pool.map(_make_batch_pair, jobs)
@@ -793,19 +828,19 @@ def cpu_baseline(prm, pattern, frames, pairs):
 
 
 def run_reference(args, torch, world, rank):
-    """The reference's own implementation of the path.  Only rank 0 works."""
+    """The reference's own implementation of the path, timed on the host cores: the
+    reference has no CPU path of its own, so this is the oracle's transcription of its
+    kernels (all host threads), one pair of the workload per step.  Parameters and the
+    pattern come from the oracle's restatement of the reference's derivation, so this
+    arm loads no engine code.  Only rank 0 works."""
     if rank != 0:
         return
-    import numpy as np
-
-    import briefmatch_gb300 as bm
     import oracle
 
     frames, flows = make_workload(rank)
-    prm = bm.BMParams.derive(W, H, UP, UP, N=NBITS)
-    pattern = prm.make_pattern(SEED)
+    p = oracle.derive_params(W, H, UP, UP, N=NBITS)
+    pattern = oracle.make_pattern(p, SEED)
     nt = oracle.num_threads()
-    p = prm.as_dict()
     seq = oracle.Sequence(p, pattern, lambda call, cnt: oracle.normals(1000 + call, 2 * cnt))
     k = 0
     seq.frame(frames[0])
@@ -831,21 +866,22 @@ def run_reference(args, torch, world, rank):
         "ms_per_step": tot / args.steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "impl": "reference", "dtype": "u32 descriptors / int16 field / f32 flow",
         "data": "synthetic (seeded generator; see bench.py)",
-        "config": {"workload": WORKLOAD % "reference", "width": W, "height": H, "upsampling": UP, "feature_length": NBITS,
-                   "step": "one pair of the sequence per step (bounded CPU sample)"},
+        "config": bench_config(world),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": nt, "kind": "port",
-                         "sample": "one pair per step of the 1024x436 sequence, %d threads" % nt},
+                         "sample": "one pair of the %dx%d sequence per step (bounded sample of the %d-pair step), "
+                                   "%d threads" % (W, H, PAIRS, nt)},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     try:
-        line["reference_cuda_build"] = reference_cuda(torch, prm, pattern, frames, args)
+        line["reference_cuda_build"] = reference_cuda(torch, p, pattern, oracle.gauss_taps(p["sigma"]), frames, args)
     except Exception as e:  # the reference kernel build is optional
         line["reference_cuda_build"] = {"unavailable": str(e)[:200]}
     print(json.dumps(line), flush=True)
 
 
-def reference_cuda(torch, prm, pattern, frames, args):
-    """The reference's kernels (compiled from its sources) over the full step on the GPU."""
+def reference_cuda(torch, params, pattern, taps, frames, args):
+    """The reference's kernels (compiled from its sources) over the full step on the GPU:
+    `params` a parameter dict, `taps` the Gaussian down-sampling taps."""
     import numpy as np
 
     from oracle import refshim
@@ -854,7 +890,14 @@ def reference_cuda(torch, prm, pattern, frames, args):
         return {"unavailable": "no GPU"}
     if not refshim.available():
         return {"unavailable": "reference kernel build (oracle/_ref) not present"}
-    pipe = refshim.RefPipeline(torch, prm.as_dict(), pattern, prm.gauss_taps())
+    # the shim launches on the legacy default stream: record the timing events there
+    with torch.cuda.stream(torch.cuda.default_stream()):
+        return _reference_cuda_timed(torch, refshim.RefPipeline(torch, params, pattern, taps), frames, args)
+
+
+def _reference_cuda_timed(torch, pipe, frames, args):
+    import numpy as np
+
     d_frames = [torch.from_numpy(f.astype(np.float32)).cuda() for f in frames]
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
 

@@ -29,6 +29,10 @@ ORACLE_BUILD = os.path.join(ORACLE_DIR, "_build")
 ORACLE_LIB = os.path.join(ORACLE_BUILD, "libbmoracle.so")
 REFSHIM_LIB = os.path.join(ORACLE_BUILD, "librefshim.so")
 REF_OUT = os.path.join(ORACLE_DIR, "_ref")
+# Where the reference's sources are read from (build_reference), if present there:
+# the environment variable BM_REFERENCE_ROOT, else the read-only checkout this recipe
+# was written against.
+REFERENCE_ROOT = os.environ.get("BM_REFERENCE_ROOT", "/root/reference")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
@@ -134,8 +138,13 @@ def build_cli(force=False):
 def build_oracle(force=False):
     os.makedirs(ORACLE_BUILD, exist_ok=True)
     src = os.path.join(ORACLE_DIR, "bm_oracle.c")
-    if force or _newer(ORACLE_LIB, [src, os.path.join(ORACLE_DIR, "bm_oracle.h")]):
-        _run(["gcc", "-O3", "-std=c11", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", "-o", ORACLE_LIB, src, "-lm"])
+    src_pat = os.path.join(ORACLE_DIR, "bm_oracle_params.cpp")
+    if force or _newer(ORACLE_LIB, [src, src_pat, os.path.join(ORACLE_DIR, "bm_oracle.h")]):
+        obj_c = os.path.join(ORACLE_BUILD, "bm_oracle.o")
+        obj_p = os.path.join(ORACLE_BUILD, "bm_oracle_params.o")
+        _run(["gcc", "-O3", "-std=c11", "-fPIC", "-fopenmp", "-ffp-contract=off", "-c", src, "-o", obj_c])
+        _run(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-c", src_pat, "-o", obj_p])
+        _run(["g++", "-shared", "-fopenmp", "-o", ORACLE_LIB, obj_c, obj_p, "-lm"])
     shim = os.path.join(ORACLE_DIR, "refshim.c")
     if os.path.exists(shim) and (force or _newer(REFSHIM_LIB, [shim])):
         _run(["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-I" + os.path.join(CUDA_HOME, "include"), "-o",
@@ -143,7 +152,7 @@ def build_oracle(force=False):
     return ORACLE_LIB
 
 
-def build_reference(ref_root="/root/reference", force=False):
+def build_reference(ref_root=None, force=False):
     """Compile the reference's own kernel sources, unmodified, to sm_103a cubins.
 
     The reference's host code needs OpenCV, Boost and libpng (absent), so only its
@@ -151,7 +160,7 @@ def build_reference(ref_root="/root/reference", force=False):
     cubins land in oracle/_ref and are loaded by oracle/refshim.c on the GPU.
     Returns the list of cubins, or [] when the reference sources are not present.
     """
-    kdir = os.path.join(ref_root, "kernels")
+    kdir = os.path.join(ref_root or REFERENCE_ROOT, "kernels")
     if not os.path.isdir(kdir):
         return []
     os.makedirs(REF_OUT, exist_ok=True)
@@ -174,7 +183,7 @@ def build_all(force=False, verbose=False):
     with ThreadPoolExecutor(max_workers=3) as ex:
         f1 = ex.submit(build_engine, force, verbose)
         f2 = ex.submit(build_oracle, force)
-        f3 = ex.submit(build_reference, "/root/reference", force)
+        f3 = ex.submit(build_reference, None, force)
         lib = f1.result()
         cli = build_cli(force)
         return lib, cli, f2.result(), f3.result()

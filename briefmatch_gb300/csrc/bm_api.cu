@@ -464,6 +464,11 @@ bm_status bm_create(const bm_params* prm, bm_ctx** out)
     if (p.sx > 32767 || p.sy > 32767)
         return fail(BM_ERR_LIMIT, "Up-sampled size %ux%u exceeds the int16 flow range.", p.sx, p.sy);
     if (p.rng != BM_RNG_XORWOW && p.rng != BM_RNG_PHILOX) return fail(BM_ERR_INVALID, "unknown rng %u", p.rng);
+    const int tri_s = bmk::trilateral_half_window(p.sEPE, p.sI, p.sS, p.sx_in, p.sy_in);
+    if (tri_s == -1) return fail(BM_ERR_INVALID, "bm_create: filter sigmas must be finite and positive");
+    if (tri_s == -2)
+        return fail(BM_ERR_LIMIT, "bm_create: trilateral window (sS = %g) is wider than twice the %ux%u frame",
+                    (double)p.sS, p.sx_in, p.sy_in);
 
     bm_ctx* c = new bm_ctx();
     c->prm = p;
@@ -479,7 +484,7 @@ bm_status bm_create(const bm_params* prm, bm_ctx** out)
     }
     c->prm.P = P;
     c->dist = std::sqrt(std::ceil((float)p.sx * 0.5f / 3.0f));  // briefmatch.cpp:271
-    c->tri_s = (int)std::ceil(2.5 * (double)std::sqrt(p.sS * p.sS));  // briefmatch_cuda.cu:266
+    c->tri_s = tri_s;  // briefmatch_cuda.cu:266
 
 #define BM_TRY(x)           \
     do {                    \

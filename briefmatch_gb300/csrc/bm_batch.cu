@@ -16,6 +16,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdarg>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <fstream>
@@ -72,7 +73,8 @@ struct BatchDev {
 
 // Bounded grid barrier for the persistent launch (all blocks co-resident by the
 // cooperative launch).  A block that waits longer than `limit` polls sets the error
-// word and every block leaves at its next barrier.
+// word and every block leaves at its next barrier.  `arrived` and `generation` are
+// cleared before every wave's launch, `error` and `where` once per step.
 struct GridSync {
     unsigned int arrived;
     unsigned int generation;
@@ -397,6 +399,10 @@ bm_status enqueue_wave(bm_batch* b, const bm_batch_schedule& s, int lo, int hi);
 // whole pipeline before the next starts.
 bm_status enqueue_step(bm_batch* b, const bm_batch_schedule& s)
 {
+    // The persistent form's barrier word: its error and phase fields start clear once
+    // per step and stay set across the step's waves (each wave resets only the arrival
+    // count and generation), so a barrier that gave up in any wave reaches check_sync.
+    if (s.persistent && !s.per_pair) BB_CUDA(cudaMemsetAsync(b->d_sync, 0, sizeof(GridSync), b->stream));
     for (const auto& w : make_waves(b, s.wave_bytes)) {
         bm_status st = enqueue_wave(b, s, w.first, w.second);
         if (st != BM_OK) return st;
@@ -559,7 +565,7 @@ bm_status enqueue_wave(bm_batch* b, const bm_batch_schedule& s, int lo, int hi)
     b->launches += 3 + 2 * (hi - lo);
     int cur = 0;
     if (s.persistent) {
-        BB_CUDA(cudaMemsetAsync(b->d_sync, 0, sizeof(GridSync), st));
+        BB_CUDA(cudaMemsetAsync(b->d_sync, 0, offsetof(GridSync, error), st));  // arrived, generation
         MatchPlan plan;
         plan.iterations = (int)b->iterations;
         plan.jfMax = (int)b->jfMax;
@@ -741,7 +747,7 @@ bm_status capture_graph(bm_batch* b)
 
 bm_status check_sync(bm_batch* b)
 {
-    if (!b->sched.persistent) return BM_OK;
+    if (!b->sched.persistent || b->sched.per_pair) return BM_OK;
     GridSync h;
     BB_CUDA(cudaMemcpyAsync(&h, b->d_sync, sizeof(h), cudaMemcpyDeviceToHost, b->stream));
     BB_CUDA(cudaStreamSynchronize(b->stream));

@@ -93,6 +93,20 @@ cudaError_t flow_to_planes(const uint32_t* flow, float* U, float* V, size_t n, c
 cudaError_t median_pass(const float* inU, const float* inV, float* outU, float* outV,
                         int dir, int fsize, int sx, int sy, cudaStream_t st);
 
+// Half window of the cross-trilateral filter, s = ceil(2.5*sqrt(sS^2))
+// (briefmatch_cuda.cu:266), for an input frame of w x h pixels.  Returns -1 when a
+// sigma is not a finite positive number, -2 when s would exceed the frame's larger
+// side (such a window adds only clamped edge samples, and its cost grows as s^2).
+inline int trilateral_half_window(float sEPE, float sI, float sS, uint32_t w, uint32_t h)
+{
+    const float big = 3.0e38f;
+    if (!(sEPE > 0 && sEPE < big) || !(sI > 0 && sI < big) || !(sS > 0 && sS < big)) return -1;
+    const double s = __builtin_ceil(2.5 * (double)__builtin_sqrtf(sS * sS));
+    const uint32_t side = w > h ? w : h;
+    if (s > (double)side) return -2;
+    return (int)s;
+}
+
 cudaError_t ensure_trilateral_smem(int s);
 cudaError_t trilateral(const float* U, const float* V, const float* Um, const float* Vm,
                        const float* I, float* Uo, float* Vo, int sx, int sy, int s,

@@ -12,6 +12,8 @@
 //   flow         uint32 per pixel, int16 nx in the low half, int16 ny in the high half
 //   cost         uint16 per pixel, the Hamming distance of the current candidate
 //                (the reference's D is cost/N)
+#include <mutex>
+
 #include "bm_device.cuh"
 
 namespace bmk {
@@ -500,17 +502,22 @@ cudaError_t median_pass(const float* inU, const float* inV, float* outU, float* 
 
 // The trilateral kernel's dynamic shared-memory opt-in, raised only when a larger
 // window than any before needs it (so launches after the first of a size make no
-// attribute call and can be captured in a graph).
+// attribute call and can be captured in a graph).  The opt-in only ever grows, under
+// a lock: contexts created on several host threads never lower it below what another
+// thread's launch was checked against.
 cudaError_t ensure_trilateral_smem(int s)
 {
+    static std::mutex mu;
     static int granted[64] = {0};
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
     const int need = (int)tri_smem_bytes(s);
-    if (dev >= 0 && dev < 64 && need <= granted[dev]) return cudaSuccess;
+    std::lock_guard<std::mutex> lock(mu);
+    if (need <= granted[dev]) return cudaSuccess;
     e = cudaFuncSetAttribute(k_trilateral_x2, cudaFuncAttributeMaxDynamicSharedMemorySize, need);
-    if (e == cudaSuccess && dev >= 0 && dev < 64) granted[dev] = need;
+    if (e == cudaSuccess) granted[dev] = need;
     return e;
 }
 

@@ -9,6 +9,7 @@
 // cross-trilateral filter of BriefMatch::process) on buffers they own.  Its
 // intermediate planes live in the fixed array below, which is part of the loaded
 // module: every GPU that loads this library holds it until the process exits.
+#include <cuda.h>  // CUcontext / CUresult types only; the driver entry points are fetched at run time
 #include <cmath>
 #include <cstdio>
 #include <mutex>
@@ -26,23 +27,62 @@ namespace {
 
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
-float* g_scratch_ptr[kMaxDevices] = {};
+// Per device: the scratch array's device address and the id of the CUDA context it
+// was looked up in.  cudaDeviceReset destroys the context and the module with it; the
+// next context has another id, so the address is looked up again there.
+struct ScratchSlot {
+    float* ptr;
+    unsigned long long ctx_id;
+};
+ScratchSlot g_slot[kMaxDevices] = {};
+
 bm_status noalloc_fail(bm_status st, const char* msg)
 {
     bmk::set_error_text(msg);
     return st;
 }
 
-// Device address of the scratch array on the current device.  Host code only
-// knows the array's host-side stand-in, so the address is looked up once per
-// device (with that device current) and cached.
+// Unique id of the calling thread's current CUDA context (0 when none is current or
+// the driver does not offer the query).  The two driver calls are fetched through the
+// runtime, so the library does not link the driver library itself.
+unsigned long long current_context_id()
+{
+    typedef CUresult (*GetCurrent)(CUcontext*);
+    typedef CUresult (*GetId)(CUcontext, unsigned long long*);
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    static bool looked_up = false;
+    if (!looked_up) {
+        void* f1 = nullptr;
+        void* f2 = nullptr;
+        cudaDriverEntryPointQueryResult q1, q2;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) == cudaSuccess &&
+            q1 == cudaDriverEntryPointSuccess &&
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) == cudaSuccess &&
+            q2 == cudaDriverEntryPointSuccess) {
+            get_current = reinterpret_cast<GetCurrent>(f1);
+            get_id = reinterpret_cast<GetId>(f2);
+        }
+        looked_up = true;
+    }
+    if (!get_current || !get_id) return 0;
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
+
+// Device address of the scratch array in the current device's context.  Host code
+// only knows the array's host-side stand-in, so the address is looked up with that
+// device current and kept for as long as the same context is current.
 bm_status scratch_on_current_device(float** out)
 {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
         return noalloc_fail(BM_ERR_CUDA, "bm_refine_noalloc: no current CUDA device");
     std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_scratch_ptr[dev]) {
+    const unsigned long long id = current_context_id();
+    if (!g_slot[dev].ptr || id == 0 || g_slot[dev].ctx_id != id) {
         void* p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_refine_scratch);
         if (e != cudaSuccess || !p) {
@@ -51,10 +91,18 @@ bm_status scratch_on_current_device(float** out)
                           cudaGetErrorString(e));
             return noalloc_fail(BM_ERR_CUDA, buf);
         }
-        g_scratch_ptr[dev] = static_cast<float*>(p);
+        g_slot[dev].ptr = static_cast<float*>(p);
+        g_slot[dev].ctx_id = current_context_id();  // the lookup makes the primary context current
     }
-    *out = g_scratch_ptr[dev];
+    *out = g_slot[dev].ptr;
     return BM_OK;
+}
+
+// True when the byte ranges [a, a + na) and [b, b + nb) overlap.
+bool overlaps(const void* a, size_t na, const void* b, size_t nb)
+{
+    const uintptr_t x = reinterpret_cast<uintptr_t>(a), y = reinterpret_cast<uintptr_t>(b);
+    return x < y + nb && y < x + na;
 }
 
 }  // namespace
@@ -80,8 +128,18 @@ bm_status bm_refine_noalloc(const float* d_u, const float* d_v, const float* d_g
         return noalloc_fail(BM_ERR_LIMIT, buf);
     }
     if (fsize > BM_MAX_MEDIAN) return noalloc_fail(BM_ERR_LIMIT, "bm_refine_noalloc: median size above 47");
-    if (!(sEPE > 0) || !(sI > 0) || !(sS > 0))
-        return noalloc_fail(BM_ERR_INVALID, "bm_refine_noalloc: filter sigmas must be positive");
+    const int tri_s = bmk::trilateral_half_window(sEPE, sI, sS, width, height);
+    if (tri_s == -1) return noalloc_fail(BM_ERR_INVALID, "bm_refine_noalloc: filter sigmas must be finite and positive");
+    if (tri_s == -2)
+        return noalloc_fail(BM_ERR_LIMIT, "bm_refine_noalloc: trilateral window wider than twice the frame");
+    // the filter reads neighbouring input samples while other threads write outputs
+    const size_t plane = (size_t)n * sizeof(float);
+    const void* ins[3] = {d_u, d_v, d_guide};
+    for (const void* in : ins)
+        if (overlaps(d_uo, plane, in, plane) || overlaps(d_vo, plane, in, plane))
+            return noalloc_fail(BM_ERR_INVALID, "bm_refine_noalloc: an output plane overlaps an input plane");
+    if (overlaps(d_uo, plane, d_vo, plane))
+        return noalloc_fail(BM_ERR_INVALID, "bm_refine_noalloc: the two output planes overlap");
     float* scratch = nullptr;
     bm_status st = scratch_on_current_device(&scratch);
     if (st != BM_OK) return st;
@@ -95,7 +153,6 @@ bm_status bm_refine_noalloc(const float* d_u, const float* d_v, const float* d_g
     // Every scratch element is written before it is read, so nothing is cleared.
     cudaError_t e = bmk::median_pass(d_u, d_v, hU, hV, 1, fs, w, h, s);
     if (e == cudaSuccess) e = bmk::median_pass(hU, hV, mU, mV, 0, fs, w, h, s);
-    const int tri_s = (int)std::ceil(2.5 * (double)std::sqrt(sS * sS));
     if (e == cudaSuccess)
         e = bmk::trilateral(d_u, d_v, mU, mV, d_guide, d_uo, d_vo, w, h, tri_s, sEPE * sEPE, sI * sI, sS * sS, s);
     if (e != cudaSuccess) {

@@ -330,10 +330,16 @@ bm_status bm_local_step(bm_ctx* ctx, uint32_t radius);
  * which every GPU that loads the library holds until the process exits, so it
  * accepts at most bm_refine_noalloc_max_pixels() (2,097,152) input pixels and
  * returns BM_ERR_LIMIT above that.  d_u, d_v: input field, d_guide: previous
- * input frame (0..255), d_uo, d_vo: output field; all width*height floats.
+ * input frame (0..255), d_uo, d_vo: output field; all width*height floats.  The
+ * output planes must not overlap the input planes or each other (BM_ERR_INVALID):
+ * the filter reads neighbouring inputs while other threads write outputs.  Sigmas
+ * must be finite and positive (BM_ERR_INVALID), and the trilateral half window
+ * ceil(2.5*sS) at most the frame's larger side (BM_ERR_LIMIT).
  * stream is a cudaStream_t (NULL = legacy default stream).  The first call on a
  * device looks up the array's device address with that device current; make that
- * first call before any stream capture.  All calls share the one array: calls whose
+ * first call before any stream capture.  The address belongs to the device's
+ * context: after cudaDeviceReset the next call looks it up again in the new
+ * context (again before any capture).  All calls share the one array: calls whose
  * work overlaps on the GPU (different streams, or host threads without ordering)
  * race on it; the array needs no clearing between calls, since every element is
  * written before it is read. */

@@ -45,6 +45,7 @@ def lib():
             "bmo_refine": (None, [vp, vp, vp, i, i, i, f, f, f, vp, vp, vp, vp]),
             "bmo_epe": (ctypes.c_double, [vp, vp, vp, vp, sz]),
             "bmo_normals": (None, [u64, sz, vp]),
+            "bmo_make_pattern": (i, [i, f, u64, vp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -193,6 +194,46 @@ def match(F1, F2, sx, sy, N, iterations, jf_max, double_prop, first, dist, norma
     lib().bmo_match(_p(_c(F1, np.uint32)), _p(_c(F2, np.uint32)), sx, sy, N, iterations, jf_max, int(bool(double_prop)),
                     int(bool(first)), dist, _p(nrm), _p(NX), _p(NY), _p(H))
     return NX, NY, H
+
+
+# BMParams::BMParams (briefmatch.h:67-84), with the engine's two additions (rng, seed)
+PARAM_DEFAULTS = dict(sx=64, sy=64, sx_in=64, sy_in=64, N=128, iterations=2, jfMax=256, P=11, fsize=13,
+                      patchArea=75.0, sigma=0.5, sEPE=0.4, sI=0.1, sS=6.0, maxmot=5.0, doubleProp=1, filter=1,
+                      tInit=1, rng=0, seed=0)
+
+
+def derive_params(width, height, ux=0.0, uy=0.0, patch_radius=3.0, sigma_downsampling=0.025, median_size=1.0,
+                  range_spatial=0.85, **overrides):
+    """OFPipeline::setParams (of_pipeline.cpp:178-190) on the BMParams defaults, in the
+    reference's types: the up-sampled size is float * unsigned truncated to unsigned,
+    the diagonals are sqrt of unsigned (32-bit) sums in double, each percentage is a
+    float product 0.01f * value before it meets the double diagonal."""
+    f32 = np.float32
+    p = dict(PARAM_DEFAULTS)
+    p.update(overrides)
+    ux, uy = f32(ux), f32(uy)
+    if ux < f32(0.1):
+        ux = f32(2.740)
+    if uy < f32(0.1):
+        uy = f32(3.052)
+    sx, sy = int(ux * f32(width)), int(uy * f32(height))
+    diag_up = float(np.sqrt(float((sx * sx + sy * sy) & 0xFFFFFFFF)))
+    diag_in = float(np.sqrt(float((width * width + height * height) & 0xFFFFFFFF)))
+    p.update(sx=sx, sy=sy, sx_in=int(width), sy_in=int(height))
+    p["patchArea"] = float(f32(float(f32(0.01) * f32(patch_radius)) * diag_up))
+    p["sigma"] = float(f32(float(f32(0.01) * f32(sigma_downsampling)) * diag_up))
+    p["fsize"] = int(2 * np.round(float(f32(0.005) * f32(median_size)) * diag_in) + 1)
+    p["sS"] = float(f32(float(f32(0.01) * f32(range_spatial)) * diag_in))
+    return p
+
+
+def make_pattern(params: dict, seed=0):
+    """The BRIEF sampling pattern for these parameters (briefmatch.cpp:124-148), 4N
+    floats, drawn from an explicit seed (bm_oracle_params.cpp)."""
+    out = np.zeros(4 * int(params["N"]), np.float32)
+    if lib().bmo_make_pattern(int(params["N"]), float(params["patchArea"]), int(seed), _p(out)) != 0:
+        raise ValueError("feature length out of range")
+    return out
 
 
 def search_dist(sx):

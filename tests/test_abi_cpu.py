@@ -118,3 +118,19 @@ def test_null_arguments():
     assert L.bm_frame(None, None, 0, None, None, 0) == bm.BM_ERR_INVALID
     assert L.bm_destroy(None) == bm.BM_OK
     assert L.bm_launch_count(None) == 0
+
+
+@pytest.mark.parametrize("w,h,u,N", [(584, 388, 1.5, 32), (1024, 436, 2.9, 128), (1920, 1080, 4.9, 512),
+                                     (512, 384, 2.9, 128), (77, 53, 2.0, 64), (640, 480, 0.0, 128)])
+def test_oracle_parameters_and_pattern_equal_the_engine(w, h, u, N):
+    """The oracle derives parameters (of_pipeline.cpp:178-190) and draws the pattern
+    (briefmatch.cpp:124-148) on its own, so that the bench's reference arm needs no
+    engine library; both restatements give the same values."""
+    e = bm.BMParams.derive(w, h, u, u, N=N)
+    o = oracle.derive_params(w, h, u, u, N=N)
+    ed = e.as_dict()
+    assert set(ed) == set(o)
+    for k in ed:
+        assert np.float32(ed[k]) == np.float32(o[k]), (k, ed[k], o[k])
+    assert np.array_equal(e.make_pattern(99), oracle.make_pattern(o, 99))
+    assert np.array_equal(e.gauss_taps(), oracle.gauss_taps(o["sigma"]))

@@ -141,3 +141,24 @@ def test_grid_barrier_gives_up():
     # the context stays usable
     x = torch.ones(4, device="cuda")
     assert float(x.sum()) == 4.0
+
+
+def test_persistent_timeout_in_any_wave_is_reported():
+    """A grid barrier that gives up in any wave of a multi-wave persistent step is
+    reported by synchronize (the barrier's error word is cleared once per step, not
+    per wave); the next step with the normal limit runs clean and matches single
+    contexts."""
+    params, frames = _batch_inputs()
+    want = _single(params, frames)
+    b = bm.Batch(params)
+    b.load_frames(b.pack_frames(frames))
+    b.set_schedule(persistent=1, per_pair=0, snake=1, use_graph=0, wave_bytes=1, spin_limit=1)  # a wave per pair
+    b.run()
+    with pytest.raises(bm.CudaException, match="status %d: " % bm.BM_ERR_TIMEOUT):
+        b.synchronize()
+    b.set_schedule(spin_limit=0)  # the default limit
+    b.run()
+    b.synchronize()
+    for (gu, gv), (wu, wv) in zip(b.read_flows(), want):
+        assert np.array_equal(gu, wu) and np.array_equal(gv, wv)
+    b.close()
