@@ -91,6 +91,9 @@ def _declare(lib):
         "bm_process": (c.c_int, [c.c_void_p, c.c_void_p]),
         "bm_swap": (c.c_int, [c.c_void_p]),
         "bm_convert": (c.c_int, [c.c_void_p, c.c_void_p, c.c_void_p]),
+        "bm_colors": (c.c_int, [c.c_void_p, c.c_void_p, c.c_int]),
+        "bm_flow_colors": (c.c_int, [c.c_void_p, c.c_void_p, c.c_uint32, c.c_uint32, c.c_float, c.c_void_p,
+                                     c.c_void_p]),
         "bm_export_field": (c.c_int, [c.c_void_p, c.c_void_p, c.c_void_p, c.c_void_p]),
         "bm_import_field": (c.c_int, [c.c_void_p, c.c_void_p, c.c_void_p, c.c_void_p]),
         "bm_normals": (c.c_int, [c.c_void_p, c.c_uint64, c.c_void_p]),
@@ -326,6 +329,17 @@ class BriefMatch:
         check(lib().bm_convert(self.ctx, u.ctypes.data, v.ctypes.data))
         return u.reshape(self.params.sy_in, self.params.sx_in), v.reshape(self.params.sy_in, self.params.sx_in)
 
+    def compute_colors(self, d_rgb=None):
+        """BriefMatch::computeColors on the GPU: the output field colour-coded, R G B
+        bytes per pixel.  With a device pointer the bytes go there; else an
+        [sy_in][sx_in][3] uint8 array is returned."""
+        if d_rgb is not None:
+            check(lib().bm_colors(self.ctx, ctypes.c_void_p(d_rgb), 1))
+            return None
+        out = np.empty((self.params.sy_in, self.params.sx_in, 3), np.uint8)
+        check(lib().bm_colors(self.ctx, out.ctypes.data, 0))
+        return out
+
     def export_field(self, d_nx, d_ny, d_dist):
         check(lib().bm_export_field(self.ctx, ctypes.c_void_p(d_nx or 0), ctypes.c_void_p(d_ny or 0),
                                     ctypes.c_void_p(d_dist or 0)))
@@ -549,6 +563,12 @@ def refine_noalloc(d_u, d_v, d_guide, d_uo, d_vo, width, height, fsize, sEPE, sI
     check(lib().bm_refine_noalloc(ctypes.c_void_p(d_u), ctypes.c_void_p(d_v), ctypes.c_void_p(d_guide),
                                   ctypes.c_void_p(d_uo), ctypes.c_void_p(d_vo), width, height, fsize, sEPE, sI, sS,
                                   ctypes.c_void_p(stream)))
+
+
+def flow_colors(d_u, d_v, width, height, max_motion, d_rgb, stream=0):
+    """Colour coding of any device field (bm_flow_colors), normalised by max_motion."""
+    check(lib().bm_flow_colors(ctypes.c_void_p(d_u), ctypes.c_void_p(d_v), width, height, max_motion,
+                               ctypes.c_void_p(d_rgb), ctypes.c_void_p(stream)))
 
 
 def version():

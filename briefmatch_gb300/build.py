@@ -47,6 +47,7 @@ ENGINE_UNITS = [
     ("bm_batch.cu", ["-use_fast_math"]),
     ("bm_api.cu", []),
     ("bm_noalloc.cu", []),
+    ("bm_color.cu", []),
     ("bm_net.cu", []),
     ("bm_params.cpp", []),
 ]

@@ -120,6 +120,10 @@ struct bm_ctx {
     uint32_t local_steps = 0, local_radius = 1;   // bm_set_local_steps
     float* d_pred = nullptr;   // [h4][w4][3]
 
+    // colour coding (bm_colors), allocated on first use
+    int* d_color_word = nullptr;    // largest vector length, float bits
+    uint8_t* d_rgb = nullptr;       // sx_in*sy_in*3 bytes
+
     struct ProfRec {
         const char* name;
         cudaEvent_t a, b;
@@ -210,7 +214,7 @@ void release(bm_ctx* c)
                     c->d_feat[0], c->d_feat[1], c->d_flow[0], c->d_flow[1], c->d_cost, c->d_flow_in_buf[0],
                     c->d_flow_in_buf[1], c->d_flow_med, c->d_flow_out,
                     c->d_tmp, c->d_pattern, c->d_taps, c->d_lx, c->d_ix, c->d_ly, c->d_iy,
-                    c->d_nnx, c->d_nny};
+                    c->d_nnx, c->d_nny, c->d_color_word, c->d_rgb};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (auto& r : c->prof_pending) {
@@ -793,6 +797,45 @@ bm_status bm_convert(bm_ctx* c, float* h_u, float* h_v)
     BM_CUDA(cudaMemcpyAsync(h_u, c->d_flow_out, b, cudaMemcpyDeviceToHost, c->stream));
     BM_CUDA(cudaMemcpyAsync(h_v, c->d_flow_out + c->npix_in, b, cudaMemcpyDeviceToHost, c->stream));
     BM_CUDA(cudaStreamSynchronize(c->stream));
+    return BM_OK;
+}
+
+bm_status bm_colors(bm_ctx* c, uint8_t* rgb, int rgb_on_device)
+{
+    if (check_ctx(c)) return BM_ERR_INVALID;
+    if (!rgb) return fail(BM_ERR_INVALID, "bm_colors: null output");
+    const size_t ni = c->npix_in;
+    if (!c->d_color_word) {
+        cudaError_t e = cudaMalloc((void**)&c->d_color_word, sizeof(int));
+        if (e != cudaSuccess) return fail(BM_ERR_NOMEM, "bm_colors: %s", cudaGetErrorString(e));
+    }
+    uint8_t* out = rgb;
+    if (!rgb_on_device) {
+        if (!c->d_rgb) {
+            cudaError_t e = cudaMalloc((void**)&c->d_rgb, 3 * ni);
+            if (e != cudaSuccess) return fail(BM_ERR_NOMEM, "bm_colors: %s", cudaGetErrorString(e));
+        }
+        out = c->d_rgb;
+    }
+    BM_CUDA(join_refine(c));
+    BM_LAUNCH(c, "flow_colors", bmk::flow_colors(c->d_flow_out, c->d_flow_out + ni, ni, c->prm.maxmot,
+                                                 c->d_color_word, out, c->stream));
+    if (!rgb_on_device) {
+        BM_CUDA(cudaMemcpyAsync(rgb, c->d_rgb, 3 * ni, cudaMemcpyDeviceToHost, c->stream));
+        BM_CUDA(cudaStreamSynchronize(c->stream));
+    }
+    return BM_OK;
+}
+
+bm_status bm_flow_colors(const float* d_u, const float* d_v, uint32_t width, uint32_t height, float max_motion,
+                         uint8_t* d_rgb, void* stream)
+{
+    if (!d_u || !d_v || !d_rgb) return fail(BM_ERR_INVALID, "bm_flow_colors: null buffer");
+    if (!(max_motion > 0) || !(max_motion < 3.0e38f))
+        return fail(BM_ERR_INVALID, "bm_flow_colors: max_motion must be a finite positive number");
+    const cudaError_t e = bmk::flow_colors(d_u, d_v, (size_t)width * height, max_motion, nullptr, d_rgb,
+                                           static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return fail(BM_ERR_CUDA, "bm_flow_colors: %s", cudaGetErrorString(e));
     return BM_OK;
 }
 

@@ -112,6 +112,13 @@ cudaError_t trilateral(const float* U, const float* V, const float* Um, const fl
                        const float* I, float* Uo, float* Vo, int sx, int sy, int s,
                        float sigmaEPE2, float sigmaI2, float sigmaS2, cudaStream_t st);
 
+// Colour coding of a flow field (u, v planes of n floats) into n*3 bytes R G B
+// (briefmatch.cpp:373-421, colorcode.cpp:52-74).  max_motion > 0 normalises by it;
+// otherwise by the largest known vector length, measured into the device word
+// d_word first.
+cudaError_t flow_colors(const float* U, const float* V, size_t n, float max_motion, int* d_word, uint8_t* rgb,
+                        cudaStream_t st);
+
 cudaError_t export_field(const uint32_t* flow, const uint16_t* cost, int16_t* nx, int16_t* ny,
                          float* dist, size_t n, int N, cudaStream_t st);
 cudaError_t import_field(const int16_t* nx, const int16_t* ny, const uint16_t* cost_in,

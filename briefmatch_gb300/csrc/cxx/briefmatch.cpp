@@ -141,9 +141,11 @@ void BriefMatch::computeColors(const float* u, const float* v, int width, int he
     }
 }
 
+// The context's own field is coloured on the GPU (bm_colors), the same arithmetic.
 void BriefMatch::computeColors()
 {
-    computeColors(m_u.data(), m_v.data(), (int)m_params.sx_in, (int)m_params.sy_in, m_vis.data());
+    if (!m_setup) throw BriefMatchException("BriefMatch is not initialized before use.");
+    bm_throw_on_error(bm_colors(m_ctx, m_vis.data(), 0));
 }
 
 void BriefMatch::printVis(std::string file)

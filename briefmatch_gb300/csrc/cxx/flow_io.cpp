@@ -299,39 +299,45 @@ bool unknown_flow(float u, float v)
 
 void flow_color(float fx, float fy, unsigned char* rgb)
 {
-    // The hue wheel: red->yellow 15 steps, yellow->green 6, green->cyan 4,
-    // cyan->blue 11, blue->magenta 13, magenta->red 6.
-    static float wheel[55][3];
+    // The hue wheel, colorcode.cpp:27-50: red->yellow 15 steps, yellow->green 6,
+    // green->cyan 4, cyan->blue 11, blue->magenta 13, magenta->red 6; each ramp is an
+    // integer division 255*i/steps.
+    static int wheel[55][3];
     static bool built = false;
     if (!built) {
         const int seg[6] = {15, 6, 4, 11, 13, 6};
         // start colour of each segment and the channel that ramps (+1 up, -1 down)
-        const float start[6][3] = {{1, 0, 0}, {1, 1, 0}, {0, 1, 0}, {0, 1, 1}, {0, 0, 1}, {1, 0, 1}};
+        const int start[6][3] = {{255, 0, 0}, {255, 255, 0}, {0, 255, 0}, {0, 255, 255}, {0, 0, 255}, {255, 0, 255}};
         const int ramp_ch[6] = {1, 0, 2, 1, 0, 2};
         const int ramp_dir[6] = {1, -1, 1, -1, 1, -1};
         int k = 0;
         for (int s = 0; s < 6; s++)
             for (int i = 0; i < seg[s]; i++, k++) {
                 for (int c = 0; c < 3; c++) wheel[k][c] = start[s][c];
-                const float t = (float)i / seg[s];
-                wheel[k][ramp_ch[s]] = ramp_dir[s] > 0 ? t : 1.0f - t;
+                wheel[k][ramp_ch[s]] = ramp_dir[s] > 0 ? 255 * i / seg[s] : 255 - 255 * i / seg[s];
             }
         built = true;
     }
+    // colorcode.cpp:57-72 with its declared types (rad, a, fk, f, col0, col1, col are
+    // float; 1.0, 2.0, pi, .75 and 255.0 are double).  The float atan2 is the correctly
+    // rounded one, as on the GPU (bm_colors).
     const int ncols = 55;
     const float rad = std::sqrt(fx * fx + fy * fy);
-    const float a = std::atan2(-fy, -fx) / (float)M_PI;
-    const float fk = (a + 1.0f) / 2.0f * (ncols - 1);
+    const float at = (float)std::atan2(-(double)fy, -(double)fx);
+    const float a = (float)((double)at / M_PI);
+    const float fk = (float)(((double)a + 1.0) / 2.0 * (ncols - 1));
     const int k0 = (int)fk;
     const int k1 = (k0 + 1) % ncols;
-    const float f = fk - k0;
+    const float f = fk - (float)k0;
     for (int c = 0; c < 3; c++) {
-        float col = (1 - f) * wheel[k0][c] + f * wheel[k1][c];
+        const float col0 = (float)(wheel[k0][c] / 255.0);
+        const float col1 = (float)(wheel[k1][c] / 255.0);
+        float col = (1 - f) * col0 + f * col1;
         if (rad <= 1)
             col = 1 - rad * (1 - col);
         else
-            col *= 0.75f;
-        rgb[c] = (unsigned char)(int)(255.0f * col);
+            col = (float)((double)col * .75);
+        rgb[c] = (unsigned char)(int)(255.0 * (double)col);
     }
 }
 

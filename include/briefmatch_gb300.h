@@ -177,6 +177,26 @@ bm_status bm_swap(bm_ctx* ctx);
 /* BriefMatch::convert, briefmatch.cpp:355-370: copy the output field to the host. */
 bm_status bm_convert(bm_ctx* ctx, float* h_u, float* h_v);
 
+/* BriefMatch::computeColors, briefmatch.cpp:373-421, with the colour wheel of
+ * util/colorcode.cpp:52-74, on the GPU: the output field (the one bm_convert
+ * returns) coloured into rgb, sx_in*sy_in*3 bytes, R G B per pixel, row-major -- the
+ * bytes of the reference's colour PNG.  Vectors are divided by params.maxmot when it
+ * is > 0, else by the largest known vector length (0 counts as 1); unknown vectors
+ * (|u| or |v| > 1e9, NaN; flowIO.cpp:35-39) are black.  rgb is a device pointer when
+ * rgb_on_device, else host memory (the call then waits for the copy).  The arithmetic
+ * follows the reference's float/double expressions without fused operations; its
+ * float atan2 is the correctly rounded one (host math libraries differ from it by one
+ * unit in the last place on some inputs, which moves a colour byte by one on rare
+ * pixels). */
+bm_status bm_colors(bm_ctx* ctx, uint8_t* rgb, int rgb_on_device);
+
+/* No counterpart in the reference (it colours only its own context's field): the same
+ * colour coding of any device field (d_u, d_v: width*height floats each) into d_rgb
+ * (width*height*3 bytes), normalised by max_motion, which must be a finite positive
+ * number; work is queued on `stream` (a cudaStream_t). */
+bm_status bm_flow_colors(const float* d_u, const float* d_v, uint32_t width, uint32_t height, float max_motion,
+                         uint8_t* d_rgb, void* stream);
+
 /* The field in the reference's layout (sint NX, NY and float D = H/N,
  * briefmatch.h:139-141), written to device arrays of sx*sy elements. */
 bm_status bm_export_field(bm_ctx* ctx, int16_t* d_nx, int16_t* d_ny, float* d_dist);

@@ -46,6 +46,7 @@ def lib():
             "bmo_epe": (ctypes.c_double, [vp, vp, vp, vp, sz]),
             "bmo_normals": (None, [u64, sz, vp]),
             "bmo_make_pattern": (i, [i, f, u64, vp]),
+            "bmo_flow_colors": (None, [vp, vp, sz, f, i, vp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -293,6 +294,17 @@ def refine(U, V, Iprev, fsize, sEPE, sI, sS):
 def epe(U, V, Ugt, Vgt):
     U, V, Ugt, Vgt = (_c(a, np.float32) for a in (U, V, Ugt, Vgt))
     return lib().bmo_epe(_p(U), _p(V), _p(Ugt), _p(Vgt), U.size)
+
+
+def flow_colors(U, V, maxmot, libm_atan2f=False):
+    """Colour coding of a flow field (briefmatch.cpp:373-421, colorcode.cpp:27-74):
+    [h][w][3] uint8, R G B."""
+    U = _c(U, np.float32)
+    V = _c(V, np.float32)
+    assert U.shape == V.shape
+    out = np.zeros(U.shape + (3,), np.uint8)
+    lib().bmo_flow_colors(_p(U), _p(V), U.size, float(maxmot), int(bool(libm_atan2f)), _p(out))
+    return out
 
 
 def normals(seed, count):

@@ -467,3 +467,78 @@ void bmo_normals(uint64_t seed, size_t count, float* out)
         if (i + 1 < count) out[i + 1] = (float)(rad * sin(2.0 * BMO_PI * u2));
     }
 }
+
+/* Colour wheel, colorcode.cpp:27-50: integer channel values from integer divisions. */
+static int colorwheel[55][3];
+static void make_colorwheel(void)
+{
+    const int RY = 15, YG = 6, GC = 4, CB = 11, BM = 13, MR = 6;
+    int k = 0, i;
+#define SETCOL(r, g, b) (colorwheel[k][0] = (r), colorwheel[k][1] = (g), colorwheel[k][2] = (b), k++)
+    for (i = 0; i < RY; i++) SETCOL(255, 255 * i / RY, 0);
+    for (i = 0; i < YG; i++) SETCOL(255 - 255 * i / YG, 255, 0);
+    for (i = 0; i < GC; i++) SETCOL(0, 255, 255 * i / GC);
+    for (i = 0; i < CB; i++) SETCOL(0, 255 - 255 * i / CB, 255);
+    for (i = 0; i < BM; i++) SETCOL(255 * i / BM, 0, 255);
+    for (i = 0; i < MR; i++) SETCOL(255, 0, 255 - 255 * i / MR);
+#undef SETCOL
+}
+
+static int unknown_flow(float u, float v)
+{
+    return fabsf(u) > 1e9f || fabsf(v) > 1e9f || u != u || v != v; /* flowIO.cpp:35-39 */
+}
+
+/* computeColor, colorcode.cpp:52-74, with its declared types (float rad, a, fk, f,
+ * col0, col1, col; the double constants 1.0, 2.0, M_PI (BMO_PI), .75, 255.0), writing R G B
+ * (the reference writes BGR at pix[2 - b]; its PNG writer swaps to RGB).  The float
+ * atan2 is the correctly rounded one (a double atan2 rounded once), or libm's atan2f
+ * when libm_atan2f is set (the reference's literal call). */
+static void compute_color(float fx, float fy, int libm_atan2f, unsigned char* pix)
+{
+    const int ncols = 55;
+    float rad = sqrtf(fx * fx + fy * fy);
+    float at = libm_atan2f ? atan2f(-fy, -fx) : (float)atan2(-(double)fy, -(double)fx);
+    float a = (float)((double)at / BMO_PI);
+    float fk = (float)(((double)a + 1.0) / 2.0 * (ncols - 1));
+    int k0 = (int)fk;
+    int k1 = (k0 + 1) % ncols;
+    float f = fk - (float)k0;
+    for (int b = 0; b < 3; b++) {
+        float col0 = (float)(colorwheel[k0][b] / 255.0);
+        float col1 = (float)(colorwheel[k1][b] / 255.0);
+        float col = (1 - f) * col0 + f * col1;
+        if (rad <= 1)
+            col = 1 - rad * (1 - col);
+        else
+            col = (float)((double)col * .75);
+        pix[b] = (unsigned char)(int)(255.0 * (double)col);
+    }
+}
+
+/* BriefMatch::computeColors, briefmatch.cpp:373-421: normalise by maxmot when it is
+ * > 0, else by the largest known vector length (0 -> 1); unknown vectors are black. */
+void bmo_flow_colors(const float* u, const float* v, size_t n, float maxmot, int libm_atan2f, unsigned char* rgb)
+{
+    static int built = 0;
+    if (!built) {
+        make_colorwheel();
+        built = 1;
+    }
+    float maxrad = -1;
+    for (size_t i = 0; i < n; i++) {
+        if (unknown_flow(u[i], v[i])) continue;
+        float rad = sqrtf(u[i] * u[i] + v[i] * v[i]);
+        if (rad > maxrad) maxrad = rad;
+    }
+    if (maxmot > 0) maxrad = maxmot;
+    if (maxrad == 0) maxrad = 1;
+#pragma omp parallel for schedule(static)
+    for (long long i = 0; i < (long long)n; i++) {
+        unsigned char* pix = rgb + 3 * i;
+        if (unknown_flow(u[i], v[i]))
+            pix[0] = pix[1] = pix[2] = 0;
+        else
+            compute_color(u[i] / maxrad, v[i] / maxrad, libm_atan2f, pix);
+    }
+}

@@ -97,6 +97,10 @@ double bmo_epe(const float* U, const float* V, const float* Ugt, const float* Vg
 /* Deterministic N(0,1) pairs for CPU-only runs (splitmix64 + Box-Muller). */
 void bmo_normals(uint64_t seed, size_t count, float* out);
 
+/* Colour coding, briefmatch.cpp:373-421 + colorcode.cpp:27-74 (R G B bytes); the float
+ * atan2 correctly rounded, or libm's atan2f when libm_atan2f is set. */
+void bmo_flow_colors(const float* u, const float* v, size_t n, float maxmot, int libm_atan2f, unsigned char* rgb);
+
 #ifdef __cplusplus
 }
 #endif

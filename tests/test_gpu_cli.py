@@ -56,9 +56,18 @@ def test_cli_bin_png_and_epe(tmp_path):
     assert len(epe_lines) == 1 and 0 <= float(epe_lines[0].split("=")[1]) < 10
     raw = np.fromfile(str(tmp_path / "o01.bin"), np.float32)
     assert raw.size == 2 * W * H and np.isfinite(raw).all()
-    run("-i", str(tmp_path / "f%02d.png"), "-f", "0:1", "-o", str(tmp_path / "c%02d.png"), "-mm", "5")
-    rgb = read_png_rgb(str(tmp_path / "c01.png"))
-    assert rgb.shape == (H, W, 3) and rgb.std() > 0
+    # the colour PNG (briefmatch.cpp:373-421, colorcode.cpp:52-74; coloured on the GPU)
+    # equals the oracle's colour coding of the same flow, byte for byte, with a fixed
+    # and with the measured motion range
+    import oracle
+
+    run("-i", str(tmp_path / "f%02d.png"), "-f", "0:1", "-o", str(tmp_path / "o%02d.flo"))
+    fu, fv = read_flo(str(tmp_path / "o01.flo"))
+    for mm, extra in ((5.0, ["-mm", "5"]), (0.0, [])):
+        run("-i", str(tmp_path / "f%02d.png"), "-f", "0:1", "-o", str(tmp_path / "c%02d.png"), *extra)
+        rgb = read_png_rgb(str(tmp_path / "c01.png"))
+        assert rgb.shape == (H, W, 3) and rgb.std() > 0
+        assert np.array_equal(rgb, oracle.flow_colors(fu, fv, mm)), mm
 
 
 def test_cli_proposal_matches_library(tmp_path):

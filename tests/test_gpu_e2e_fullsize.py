@@ -1,0 +1,203 @@
+"""End to end at the benchmark workloads' sizes: the whole matched field (NX, NY,
+Hamming cost) on the up-sampled grid bit for bit, the down-sampled flow bit for
+bit and the refined flow within 1e-4 px, engine against the oracle fed the
+engine's up-sampled frames, random normals and nearest-neighbour tables (the frame
+loop of of_pipeline.cpp:241-333 and briefmatch.cpp:248-352):
+
+- 584x388 u1.5 N32, one pair (the reference's small case);
+- 1024x436 u2.9 N128, a three-frame sequence (zero init, then temporal init),
+  pipelined frames as the benchmark runs them, once plain and once seeded by the
+  committed learned proposal at the benchmark's calibrated schedule (1 iteration,
+  jump maximum 128);
+- three pairs of the 64-pair uneven batch (the largest, the smallest and the most
+  elongated), run as a batch and compared with the oracle directly;
+- a 1920x256 crop with the 1920x1080 u4.9 N512 parameters (9408x1254 up-sampled,
+  64-byte descriptors, pattern offsets up to 158 px); the trilateral filter there
+  has 8836 taps per pixel, where the oracle's single float sum over all taps (the
+  reference's order) is itself ~1.1e-4 px from float64, so the bar is 3e-4 px.
+
+The oracle runs on all host threads; the whole file takes about a minute there.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import briefmatch_gb300 as bm
+import oracle
+from bmtest import engine_field, engine_normals
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("no GPU", allow_module_level=True)
+
+from briefmatch_gb300 import learn, synth  # noqa: E402
+
+FLOW_TOL = 1e-4
+FLOW_TOL_8836_TAPS = 3e-4
+BATCH_SEED = 20261204  # the batched workload's seed (bench.py)
+
+
+def _dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def _engine(prm, pattern, pipelined=False, net=None, schedule=None):
+    eng = bm.BriefMatch(prm)
+    eng.setup()
+    eng.set_pattern(pattern)
+    eng.set_stream(torch.cuda.current_stream().cuda_stream)
+    if net is not None:
+        bm.set_proposal(eng, net, 0.5, schedule[0], schedule[1])
+    if pipelined:
+        eng.set_pipelined(True)
+    return eng
+
+
+def _compare_sequence(eng, prm, pattern, frames, proposal=None, tol=FLOW_TOL):
+    """Feed `frames` to the engine (bm_frame) and to the oracle's frame loop; every
+    pair's field, down-sampled flow and refined flow must agree."""
+    normals_cache = {}
+
+    def normals_fn(call, n):
+        if call not in normals_cache:
+            normals_cache[call] = engine_normals(eng, call)
+        return normals_cache[call]
+
+    seq = oracle.Sequence(prm.as_dict(), pattern, normals_fn, nn=eng.nn_indices(), proposal=proposal)
+    pairs = 0
+    for k, f in enumerate(frames):
+        d = _dev(f)
+        u = torch.empty(prm.sy_in, prm.sx_in, device="cuda")
+        v = torch.empty(prm.sy_in, prm.sx_in, device="cuda")
+        eng.frame(d.data_ptr(), True, u.data_ptr(), v.data_ptr(), True)
+        eng.synchronize()
+        torch.cuda.synchronize()
+        nx, ny, cost, _ = engine_field(eng)
+        uv_in = eng.read_buffer(bm.BM_BUF_FLOW_IN, np.float32).reshape(2, prm.sy_in, prm.sx_in)
+        d_up = torch.empty(prm.sy, prm.sx, device="cuda")
+        eng.upsample_u8(d.data_ptr(), d_up.data_ptr())
+        torch.cuda.synchronize()
+        o = seq.frame(f, up=d_up.cpu().numpy())
+        if k == 0:
+            assert o is None
+            continue
+        pairs += 1
+        assert np.array_equal(nx, seq.NX), ("NX", k, int((nx != seq.NX).sum()))
+        assert np.array_equal(ny, seq.NY), ("NY", k, int((ny != seq.NY).sum()))
+        assert np.array_equal(cost, seq.H), ("cost", k)
+        assert np.array_equal(uv_in[0], seq.U) and np.array_equal(uv_in[1], seq.V), ("down-sampled", k)
+        err = max(float(np.abs(u.cpu().numpy() - o[0]).max()), float(np.abs(v.cpu().numpy() - o[1]).max()))
+        assert err <= tol, ("refined", k, err)
+        # the field is a real match, not a trivially equal one
+        assert float(cost.mean()) < 0.25 * prm.N
+    return pairs
+
+
+def test_cfg1_pair_584x388_u15_n32():
+    W, H = 584, 388
+    prm = bm.BMParams.derive(W, H, 1.5, 1.5, N=32)
+    pattern = prm.make_pattern(20261203)
+    f1, f2, _, _ = synth.make_pair(101, W, H, vmax=10.0)
+    eng = _engine(prm, pattern)
+    assert _compare_sequence(eng, prm, pattern, [f1, f2]) == 1
+    eng.clean()
+
+
+def test_cfg2_sequence_1024x436_u29_n128_plain():
+    W, H = 1024, 436
+    prm = bm.BMParams.derive(W, H, 2.9, 2.9, N=128)
+    pattern = prm.make_pattern(20261203)
+    frames, _ = synth.make_sequence(20261203, W, H, 3, vmax=15.0)
+    eng = _engine(prm, pattern, pipelined=True)
+    assert _compare_sequence(eng, prm, pattern, frames) == 2
+    eng.clean()
+
+
+def test_cfg2_sequence_1024x436_u29_n128_learned_seeded():
+    W, H = 1024, 436
+    h4, w4 = H // 4, W // 4
+    it, jf = 1, 128
+    prm = bm.BMParams.derive(W, H, 2.9, 2.9, N=128)
+    pattern = prm.make_pattern(20261203)
+    frames, _ = synth.make_sequence(20261203, W, H, 3, vmax=15.0)
+    net = learn.load_net(learn.DEFAULT_WEIGHTS, 1, h4, w4)
+    eng = _engine(prm, pattern, pipelined=True, net=net, schedule=(it, jf))
+
+    def pred_fn(prev_u8, cur_u8):
+        d0, d1 = _dev(prev_u8), _dev(cur_u8)
+        out = torch.empty(h4, w4, 3, device="cuda")
+        st = torch.cuda.current_stream().cuda_stream
+        net.prepare(0, d0.data_ptr(), d1.data_ptr(), W, H, st)
+        net.forward(1, h4, w4, out.data_ptr(), st)
+        torch.cuda.synchronize()
+        return out.cpu().numpy()
+
+    assert _compare_sequence(eng, prm, pattern, frames, proposal=(pred_fn, 0.0, it, jf)) == 2
+    assert eng.rng_position() == 2 * it
+    eng.clean()
+    net.close()
+
+
+def _batch_picks():
+    sizes = synth.make_batch_sizes(BATCH_SEED, count=64)
+    area = [w * h for w, h in sizes]
+    aspect = [max(w / h, h / w) for w, h in sizes]
+    picks = []
+    for k in (int(np.argmax(area)), int(np.argmin(area)), int(np.argmax(aspect))):
+        if k not in picks:
+            picks.append(k)
+    return [(k, sizes[k]) for k in picks]
+
+
+def test_batched_pairs_against_oracle():
+    picks = _batch_picks()
+    params = [bm.BMParams.derive(w, h, 2.9, 2.9, N=128) for _, (w, h) in picks]
+    data = [synth.make_pair(BATCH_SEED + k, w, h, vmax=15.0) for k, (w, h) in picks]
+    b = bm.Batch(params)
+    b.set_stream(torch.cuda.current_stream().cuda_stream)
+    b.load_frames(b.pack_frames([(d[0], d[1]) for d in data]))
+    b.set_schedule(per_pair=1, persistent=0, snake=1, use_graph=1, streams=2)
+    b.run()
+    b.synchronize()
+    flows = b.read_flows()
+    b.close()
+    for (k, (w, h)), prm, d, (gu, gv) in zip(picks, params, data, flows):
+        # a fresh context of the same size supplies the device-side tables and normals
+        # the oracle consumes; a batch pair uses its default pattern (seed 0)
+        pattern = prm.make_pattern(0)
+        eng = _engine(prm, pattern)
+        normals = [engine_normals(eng, c) for c in range(prm.iterations)]
+        nn = eng.nn_indices()
+        ups = []
+        for f in (d[0], d[1]):
+            dd = _dev(f)
+            d_up = torch.empty(prm.sy, prm.sx, device="cuda")
+            eng.upsample_u8(dd.data_ptr(), d_up.data_ptr())
+            torch.cuda.synchronize()
+            ups.append(d_up.cpu().numpy())
+        eng.clean()
+        seq = oracle.Sequence(prm.as_dict(), pattern, lambda c, n: normals[c], nn=nn)
+        seq.frame(d[0], up=ups[0])
+        ou, ov = seq.frame(d[1], up=ups[1])
+        err = max(float(np.abs(gu - ou).max()), float(np.abs(gv - ov).max()))
+        assert err <= FLOW_TOL, (k, w, h, err)
+        epe = float(np.mean(np.hypot(gu - d[2], gv - d[3])))
+        assert epe < 3.0, (k, w, h, epe)
+
+
+def test_cfg3_crop_1920x256_u49_n512():
+    """The 1920x1080 u4.9 N512 parameters (patch radius, filter sizes) on a 1920x256
+    crop, so the oracle follows over the whole field."""
+    full = bm.BMParams.derive(1920, 1080, 4.9, 4.9, N=512)
+    prm = bm.BMParams.derive(1920, 1080, 4.9, 4.9, N=512)
+    prm.sy_in = 256
+    prm.sy = int(np.float32(4.9) * np.float32(256))
+    assert prm.sx == full.sx and prm.patchArea == full.patchArea and prm.sS == full.sS
+    pattern = prm.make_pattern(20261203)
+    f1, f2, _, _ = synth.make_pair(303, 1920, 256, vmax=24.0)
+    eng = _engine(prm, pattern)
+    assert _compare_sequence(eng, prm, pattern, [f1, f2], tol=FLOW_TOL_8836_TAPS) == 1
+    eng.clean()
