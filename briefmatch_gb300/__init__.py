@@ -135,6 +135,11 @@ def _declare(lib):
         "bm_batch_launch_count": (c.c_uint64, [c.c_void_p]),
         "bm_batch_autotune": (c.c_int, [c.c_void_p, c.c_char_p, c.c_int, c.c_char_p, c.c_size_t]),
         "bm_selftest_barrier": (c.c_int, [c.c_uint32, c.c_uint32, c.c_uint64, P(c.c_int)]),
+        "bm_debug_fail_alloc": (None, [c.c_uint64]),
+        "bm_debug_alloc_count": (c.c_uint64, []),
+        "bm_debug_live_allocs": (c.c_int64, []),
+        "bm_debug_guard_bands": (None, [c.c_int]),
+        "bm_debug_check_guards": (c.c_int, [P(c.c_uint64)]),
         "bm_last_error": (c.c_char_p, []),
         "bm_version": (c.c_char_p, []),
     }
@@ -569,6 +574,27 @@ def flow_colors(d_u, d_v, width, height, max_motion, d_rgb, stream=0):
     """Colour coding of any device field (bm_flow_colors), normalised by max_motion."""
     check(lib().bm_flow_colors(ctypes.c_void_p(d_u), ctypes.c_void_p(d_v), width, height, max_motion,
                                ctypes.c_void_p(d_rgb), ctypes.c_void_p(stream)))
+
+
+def debug_fail_alloc(k):
+    """Test hook: the k-th device allocation from now on fails (0 disables)."""
+    lib().bm_debug_fail_alloc(k)
+
+
+def debug_live_allocs():
+    return int(lib().bm_debug_live_allocs())
+
+
+def debug_guard_bands(on):
+    """Test hook: guard bands around every device buffer allocated while on."""
+    lib().bm_debug_guard_bands(int(bool(on)))
+
+
+def debug_check_guards():
+    """Number of guarded buffers checked; raises if a guard band was overwritten."""
+    n = ctypes.c_uint64(0)
+    check(lib().bm_debug_check_guards(ctypes.byref(n)))
+    return n.value
 
 
 def version():

@@ -50,6 +50,7 @@ ENGINE_UNITS = [
     ("bm_color.cu", []),
     ("bm_net.cu", []),
     ("bm_params.cpp", []),
+    ("bm_alloc.cpp", []),
 ]
 
 

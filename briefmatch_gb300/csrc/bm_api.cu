@@ -200,7 +200,7 @@ bm_status dev_alloc(T** p, size_t count)
 {
     *p = nullptr;
     if (count == 0) count = 1;
-    cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+    cudaError_t e = bmk::device_malloc((void**)p, count * sizeof(T));
     if (e != cudaSuccess) {
         *p = nullptr;
         return fail(BM_ERR_NOMEM, "cudaMalloc of %zu bytes failed: %s", count * sizeof(T), cudaGetErrorString(e));
@@ -216,7 +216,7 @@ void release(bm_ctx* c)
                     c->d_tmp, c->d_pattern, c->d_taps, c->d_lx, c->d_ix, c->d_ly, c->d_iy,
                     c->d_nnx, c->d_nny, c->d_color_word, c->d_rgb};
     for (void* p : ptrs)
-        if (p) cudaFree(p);
+        if (p) bmk::device_free(p);
     for (auto& r : c->prof_pending) {
         cudaEventDestroy(r.a);
         cudaEventDestroy(r.b);
@@ -415,10 +415,10 @@ bm_status set_pattern_impl(bm_ctx* c, const float* h_pattern)
         if (st != BM_OK) return st;
         const cudaError_t e = cudaStreamSynchronize(c->stream);
         if (e != cudaSuccess) {
-            cudaFree(fresh);
+            bmk::device_free(fresh);
             return fail(BM_ERR_CUDA, "bm_set_pattern: %s", cudaGetErrorString(e));
         }
-        if (c->d_upad) cudaFree(c->d_upad);
+        if (c->d_upad) bmk::device_free(c->d_upad);
         c->d_upad = fresh;
         c->up_margin = rmax;
         c->upad_valid = false;
@@ -806,13 +806,13 @@ bm_status bm_colors(bm_ctx* c, uint8_t* rgb, int rgb_on_device)
     if (!rgb) return fail(BM_ERR_INVALID, "bm_colors: null output");
     const size_t ni = c->npix_in;
     if (!c->d_color_word) {
-        cudaError_t e = cudaMalloc((void**)&c->d_color_word, sizeof(int));
+        cudaError_t e = bmk::device_malloc((void**)&c->d_color_word, sizeof(int));
         if (e != cudaSuccess) return fail(BM_ERR_NOMEM, "bm_colors: %s", cudaGetErrorString(e));
     }
     uint8_t* out = rgb;
     if (!rgb_on_device) {
         if (!c->d_rgb) {
-            cudaError_t e = cudaMalloc((void**)&c->d_rgb, 3 * ni);
+            cudaError_t e = bmk::device_malloc((void**)&c->d_rgb, 3 * ni);
             if (e != cudaSuccess) return fail(BM_ERR_NOMEM, "bm_colors: %s", cudaGetErrorString(e));
         }
         out = c->d_rgb;

@@ -698,7 +698,7 @@ bm_status ensure_branches(bm_batch* b, int k)
             }
             b->net_copy.push_back(n);
             float* pr = nullptr;
-            if (cudaMalloc((void**)&pr, cells * 3 * sizeof(float)) != cudaSuccess)
+            if (bmk::device_malloc((void**)&pr, cells * 3 * sizeof(float)) != cudaSuccess)
                 return bfail(BM_ERR_NOMEM, "bm_batch: prediction buffer allocation failed");
             b->pred_copy.push_back(pr);
         }
@@ -709,7 +709,7 @@ bm_status ensure_branches(bm_batch* b, int k)
 void drop_net_copies(bm_batch* b)
 {
     for (bm_net* n : b->net_copy) bm_net_destroy(n);
-    for (float* p : b->pred_copy) cudaFree(p);
+    for (float* p : b->pred_copy) bmk::device_free(p);
     b->net_copy.clear();
     b->pred_copy.clear();
 }
@@ -895,14 +895,14 @@ bm_status bm_batch_create(const bm_params* pairs, uint32_t count, bm_batch** out
         o.nny = take((size_t)p.sy_in * 4);
     }
     b->arena_bytes = cursor;
-    cudaError_t e = cudaMalloc((void**)&b->arena, b->arena_bytes);
+    cudaError_t e = bmk::device_malloc((void**)&b->arena, b->arena_bytes);
     if (e != cudaSuccess) {
         delete b;
         return bfail(BM_ERR_NOMEM, "bm_batch_create: cudaMalloc of %zu bytes failed: %s", cursor, cudaGetErrorString(e));
     }
     e = cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
-        cudaFree(b->arena);
+        bmk::device_free(b->arena);
         delete b;
         return bfail(BM_ERR_CUDA, "bm_batch_create: %s", cudaGetErrorString(e));
     }
@@ -987,9 +987,9 @@ bm_status bm_batch_create(const bm_params* pairs, uint32_t count, bm_batch** out
     if (b->filter && b->tri_smem > 220 * 1024)
         return fail_clean(bfail(BM_ERR_LIMIT, "bm_batch_create: spatial window %d too large for the batched filter",
                                 b->max_tri_s));
-    if (cudaMalloc((void**)&b->d_pairs, count * sizeof(PairDev)) != cudaSuccess ||
-        cudaMalloc((void**)&b->d_pre, 3 * (count + 1) * sizeof(unsigned int)) != cudaSuccess ||
-        cudaMalloc((void**)&b->d_sync, sizeof(GridSync)) != cudaSuccess)
+    if (bmk::device_malloc((void**)&b->d_pairs, count * sizeof(PairDev)) != cudaSuccess ||
+        bmk::device_malloc((void**)&b->d_pre, 3 * (count + 1) * sizeof(unsigned int)) != cudaSuccess ||
+        bmk::device_malloc((void**)&b->d_sync, sizeof(GridSync)) != cudaSuccess)
         return fail_clean(bfail(BM_ERR_NOMEM, "bm_batch_create: descriptor allocation failed"));
     std::vector<unsigned int> pre;
     pre.insert(pre.end(), b->pre_up.begin(), b->pre_up.end());
@@ -1028,11 +1028,11 @@ bm_status bm_batch_destroy(bm_batch* b)
     if (!b) return BM_OK;
     if (b->stream) cudaStreamSynchronize(b->stream);
     destroy_graph(b);
-    if (b->arena) cudaFree(b->arena);
-    if (b->d_pairs) cudaFree(b->d_pairs);
-    if (b->d_pre) cudaFree(b->d_pre);
-    if (b->d_sync) cudaFree(b->d_sync);
-    if (b->d_pred) cudaFree(b->d_pred);
+    if (b->arena) bmk::device_free(b->arena);
+    if (b->d_pairs) bmk::device_free(b->d_pairs);
+    if (b->d_pre) bmk::device_free(b->d_pre);
+    if (b->d_sync) bmk::device_free(b->d_sync);
+    if (b->d_pred) bmk::device_free(b->d_pred);
     drop_net_copies(b);
     for (cudaStream_t st : b->branch) cudaStreamDestroy(st);
     for (cudaEvent_t ev : b->branch_done) cudaEventDestroy(ev);
@@ -1202,7 +1202,7 @@ bm_status bm_batch_set_proposal(bm_batch* b, bm_net* net, float conf_threshold, 
             if (p.sx_in < 4 || p.sy_in < 4) return bfail(BM_ERR_LIMIT, "bm_batch_set_proposal: frame too small");
             cells = std::max(cells, (size_t)(p.sx_in / 4) * (p.sy_in / 4));
         }
-        if (!b->d_pred && cudaMalloc((void**)&b->d_pred, cells * 3 * sizeof(float)) != cudaSuccess)
+        if (!b->d_pred && bmk::device_malloc((void**)&b->d_pred, cells * 3 * sizeof(float)) != cudaSuccess)
             return bfail(BM_ERR_NOMEM, "bm_batch_set_proposal: prediction buffer allocation failed");
         b->sched.per_pair = 1;
         b->sched.persistent = 0;
@@ -1344,14 +1344,14 @@ bm_status bm_selftest_barrier(uint32_t blocks, uint32_t expect, uint64_t spin_li
 {
     if (!timed_out || blocks == 0 || blocks > 64) return bfail(BM_ERR_INVALID, "bm_selftest_barrier: bad argument");
     GridSync* gs = nullptr;
-    BB_CUDA(cudaMalloc((void**)&gs, sizeof(GridSync)));
+    BB_CUDA(cudaMalloc((void**)&gs, sizeof(GridSync)));  // self-test scratch, not engine state
     cudaMemset(gs, 0, sizeof(GridSync));
     void* args[] = {(void*)&gs, (void*)&expect, (void*)&spin_limit};
     cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_barrier_selftest, dim3(blocks), dim3(32), args, 0, 0);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     GridSync h{};
     if (e == cudaSuccess) e = cudaMemcpy(&h, gs, sizeof(h), cudaMemcpyDeviceToHost);
-    cudaFree(gs);
+    cudaFree(gs);  // self-test scratch
     if (e != cudaSuccess) return bfail(BM_ERR_CUDA, "bm_selftest_barrier: %s", cudaGetErrorString(e));
     *timed_out = h.error ? 1 : 0;
     return h.error ? bfail(BM_ERR_TIMEOUT, "grid barrier gave up after %llu polls", (unsigned long long)spin_limit)

@@ -12,6 +12,11 @@ namespace bmk {
 // Sets the text bm_last_error() returns on this thread.
 void set_error_text(const char* msg);
 
+// The engine's device allocator (bm_alloc.cpp): cudaMalloc/cudaFree behind the test
+// hooks bm_debug_fail_alloc and bm_debug_guard_bands.
+cudaError_t device_malloc(void** p, size_t bytes);
+void device_free(void* p);
+
 // Random-search stream position for one launch (briefmatch_cuda.cu:237-241).
 struct RsArgs {
     int enabled;                 // fuse a random-search candidate into the launch

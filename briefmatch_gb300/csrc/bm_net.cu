@@ -559,19 +559,19 @@ bm_status bm_net_create(uint32_t max_batch, uint32_t max_h4, uint32_t max_w4, bm
     }
     n->nparam = off;
     const size_t px = (size_t)max_batch * max_h4 * max_w4;
-    bool ok = cudaMalloc((void**)&n->d_master, off * 4) == cudaSuccess &&
-              cudaMalloc((void**)&n->d_grad, off * 4) == cudaSuccess &&
-              cudaMalloc((void**)&n->d_m, off * 4) == cudaSuccess && cudaMalloc((void**)&n->d_v, off * 4) == cudaSuccess &&
-              cudaMalloc((void**)&n->d_in, px * NIN * 2) == cudaSuccess &&
-              cudaMalloc((void**)&n->d_out, px * 3 * 4) == cudaSuccess &&
-              cudaMalloc((void**)&n->d_loss, 4 * 4) == cudaSuccess &&
-              cudaMalloc((void**)&n->d_dy[0], px * 32 * 2) == cudaSuccess &&
-              cudaMalloc((void**)&n->d_dy[1], px * 32 * 2) == cudaSuccess;
-    for (int l = 0; ok && l < NL - 1; l++) ok = cudaMalloc((void**)&n->d_act[l], px * 32 * 2) == cudaSuccess;
+    bool ok = bmk::device_malloc((void**)&n->d_master, off * 4) == cudaSuccess &&
+              bmk::device_malloc((void**)&n->d_grad, off * 4) == cudaSuccess &&
+              bmk::device_malloc((void**)&n->d_m, off * 4) == cudaSuccess && bmk::device_malloc((void**)&n->d_v, off * 4) == cudaSuccess &&
+              bmk::device_malloc((void**)&n->d_in, px * NIN * 2) == cudaSuccess &&
+              bmk::device_malloc((void**)&n->d_out, px * 3 * 4) == cudaSuccess &&
+              bmk::device_malloc((void**)&n->d_loss, 4 * 4) == cudaSuccess &&
+              bmk::device_malloc((void**)&n->d_dy[0], px * 32 * 2) == cudaSuccess &&
+              bmk::device_malloc((void**)&n->d_dy[1], px * 32 * 2) == cudaSuccess;
+    for (int l = 0; ok && l < NL - 1; l++) ok = bmk::device_malloc((void**)&n->d_act[l], px * 32 * 2) == cudaSuccess;
     for (int l = 0; ok && l < NL; l++) {
         const int coutp16 = COUT_P[l] < 16 ? 16 : COUT_P[l];
-        ok = cudaMalloc((void**)&n->d_wf[l], (size_t)9 * COUT_P[l] * CIN_P[l] * 2) == cudaSuccess &&
-             cudaMalloc((void**)&n->d_wb[l], (size_t)9 * CIN_P[l] * coutp16 * 2) == cudaSuccess;
+        ok = bmk::device_malloc((void**)&n->d_wf[l], (size_t)9 * COUT_P[l] * CIN_P[l] * 2) == cudaSuccess &&
+             bmk::device_malloc((void**)&n->d_wb[l], (size_t)9 * CIN_P[l] * coutp16 * 2) == cudaSuccess;
     }
     if (!ok) {
         bm_net_destroy(n);
@@ -608,11 +608,11 @@ bm_status bm_net_destroy(bm_net* n)
     if (!n) return BM_OK;
     void* ptrs[] = {n->d_master, n->d_grad, n->d_m, n->d_v, n->d_in, n->d_out, n->d_loss, n->d_dy[0], n->d_dy[1]};
     for (void* q : ptrs)
-        if (q) cudaFree(q);
+        if (q) bmk::device_free(q);
     for (int l = 0; l < NL; l++) {
-        if (n->d_wf[l]) cudaFree(n->d_wf[l]);
-        if (n->d_wb[l]) cudaFree(n->d_wb[l]);
-        if (l < NL - 1 && n->d_act[l]) cudaFree(n->d_act[l]);
+        if (n->d_wf[l]) bmk::device_free(n->d_wf[l]);
+        if (n->d_wb[l]) bmk::device_free(n->d_wb[l]);
+        if (l < NL - 1 && n->d_act[l]) bmk::device_free(n->d_act[l]);
     }
     delete n;
     return BM_OK;

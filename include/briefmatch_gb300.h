@@ -286,6 +286,24 @@ bm_status bm_batch_set_local_steps(bm_batch* b, uint32_t count, uint32_t first_r
  * every block gives up, *timed_out is set and BM_ERR_TIMEOUT returned. */
 bm_status bm_selftest_barrier(uint32_t blocks, uint32_t expect, uint64_t spin_limit, int* timed_out);
 
+/* ---- test hooks on the device allocator (no counterpart in the reference) ----------
+ * The reference turns any CUDA failure into a CudaException (HANDLE_ERROR,
+ * util_cuda.h:102-112); these hooks let tests reach the engine's BM_ERR_NOMEM paths
+ * and catch out-of-bounds writes.  All are host-only and off by default. */
+/* The k-th device allocation of the library from now on fails as if the device were
+ * out of memory (k = 0: none fails). */
+void bm_debug_fail_alloc(uint64_t k);
+/* Device allocations made so far, and those made and not yet freed. */
+uint64_t bm_debug_alloc_count(void);
+int64_t bm_debug_live_allocs(void);
+/* While on, new allocations carry 256-byte guard bands before and after the buffer
+ * (the buffer too starts filled with the guard byte 0xA5). */
+void bm_debug_guard_bands(int on);
+/* Synchronises the device and checks every live guard band: BM_ERR_STATE (with the
+ * buffer and byte in bm_last_error) if a kernel wrote into one; *checked (may be
+ * NULL) receives the number of guarded buffers. */
+bm_status bm_debug_check_guards(uint64_t* checked);
+
 /* ---- learned flow proposal ---------------------------------------------------------- */
 
 /* No counterpart in the reference.  A 6-layer 3x3 convolutional network (32->32 x5,

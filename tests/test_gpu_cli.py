@@ -63,7 +63,8 @@ def test_cli_bin_png_and_epe(tmp_path):
 
     run("-i", str(tmp_path / "f%02d.png"), "-f", "0:1", "-o", str(tmp_path / "o%02d.flo"))
     fu, fv = read_flo(str(tmp_path / "o01.flo"))
-    for mm, extra in ((5.0, ["-mm", "5"]), (0.0, [])):
+    # no -mm: BMParams' default maxmot (5, briefmatch.h:83); -mm 0: the measured range
+    for mm, extra in ((5.0, []), (2.5, ["-mm", "2.5"]), (0.0, ["-mm", "0"])):
         run("-i", str(tmp_path / "f%02d.png"), "-f", "0:1", "-o", str(tmp_path / "c%02d.png"), *extra)
         rgb = read_png_rgb(str(tmp_path / "c01.png"))
         assert rgb.shape == (H, W, 3) and rgb.std() > 0

@@ -12,9 +12,14 @@ loop of of_pipeline.cpp:241-333 and briefmatch.cpp:248-352):
 - three pairs of the 64-pair uneven batch (the largest, the smallest and the most
   elongated), run as a batch and compared with the oracle directly;
 - a 1920x256 crop with the 1920x1080 u4.9 N512 parameters (9408x1254 up-sampled,
-  64-byte descriptors, pattern offsets up to 158 px); the trilateral filter there
-  has 8836 taps per pixel, where the oracle's single float sum over all taps (the
-  reference's order) is itself ~1.1e-4 px from float64, so the bar is 3e-4 px.
+  64-byte descriptors, pattern offsets up to 158 px).
+
+Refined-flow bar: 1e-4 px against the oracle up to the 2304 taps per pixel of the
+1024x436 workload.  Larger frames have wider windows (8464 taps for the batch's
+1852x1052 pair, 8836 at 1920 px width), where the oracle's single float sum over all
+taps -- the reference's order -- is itself up to ~1.1e-4 px from float64; there the
+engine must be within 3e-4 px of the oracle and within 1e-4 px of a float64
+evaluation of the filter on a band of rows.
 
 The oracle runs on all host threads; the whole file takes about a minute there.
 """
@@ -25,7 +30,7 @@ import pytest
 
 import briefmatch_gb300 as bm
 import oracle
-from bmtest import engine_field, engine_normals
+from bmtest import engine_field, engine_normals, trilateral_f64
 
 pytestmark = pytest.mark.gpu
 
@@ -36,7 +41,7 @@ if not torch.cuda.is_available():
 from briefmatch_gb300 import learn, synth  # noqa: E402
 
 FLOW_TOL = 1e-4
-FLOW_TOL_8836_TAPS = 3e-4
+FLOW_TOL_WIDE = 3e-4   # against the oracle's float order when the window exceeds 48x48 taps
 BATCH_SEED = 20261204  # the batched workload's seed (bench.py)
 
 
@@ -56,7 +61,23 @@ def _engine(prm, pattern, pipelined=False, net=None, schedule=None):
     return eng
 
 
-def _compare_sequence(eng, prm, pattern, frames, proposal=None, tol=FLOW_TOL):
+def _check_refined(prm, u, v, ou, ov, U, V, Um, Vm, guide, what):
+    """Refined flow (u, v) against the oracle's (ou, ov) and, for windows wider than
+    48x48 taps, against a float64 evaluation on a band of rows of the oracle's
+    down-sampled and median inputs (both bit-exact with the engine's)."""
+    s = int(np.ceil(2.5 * prm.sS))
+    err = max(float(np.abs(u - ou).max()), float(np.abs(v - ov).max()))
+    if s <= 24:
+        assert err <= FLOW_TOL, (what, err)
+        return
+    assert err <= FLOW_TOL_WIDE, (what, err)
+    r0, rows = prm.sy_in // 2, 3
+    eu, ev = trilateral_f64(U, V, Um, Vm, guide, r0, rows, s, prm.sEPE, prm.sI, prm.sS)
+    err64 = max(float(np.abs(u[r0:r0 + rows] - eu).max()), float(np.abs(v[r0:r0 + rows] - ev).max()))
+    assert err64 <= FLOW_TOL, (what, "vs float64", err64)
+
+
+def _compare_sequence(eng, prm, pattern, frames, proposal=None):
     """Feed `frames` to the engine (bm_frame) and to the oracle's frame loop; every
     pair's field, down-sampled flow and refined flow must agree."""
     normals_cache = {}
@@ -89,8 +110,8 @@ def _compare_sequence(eng, prm, pattern, frames, proposal=None, tol=FLOW_TOL):
         assert np.array_equal(ny, seq.NY), ("NY", k, int((ny != seq.NY).sum()))
         assert np.array_equal(cost, seq.H), ("cost", k)
         assert np.array_equal(uv_in[0], seq.U) and np.array_equal(uv_in[1], seq.V), ("down-sampled", k)
-        err = max(float(np.abs(u.cpu().numpy() - o[0]).max()), float(np.abs(v.cpu().numpy() - o[1]).max()))
-        assert err <= tol, ("refined", k, err)
+        _check_refined(prm, u.cpu().numpy(), v.cpu().numpy(), o[0], o[1], seq.U, seq.V, seq.Um, seq.Vm,
+                       frames[k - 1], ("refined", k))
         # the field is a real match, not a trivially equal one
         assert float(cost.mean()) < 0.25 * prm.N
     return pairs
@@ -182,8 +203,7 @@ def test_batched_pairs_against_oracle():
         seq = oracle.Sequence(prm.as_dict(), pattern, lambda c, n: normals[c], nn=nn)
         seq.frame(d[0], up=ups[0])
         ou, ov = seq.frame(d[1], up=ups[1])
-        err = max(float(np.abs(gu - ou).max()), float(np.abs(gv - ov).max()))
-        assert err <= FLOW_TOL, (k, w, h, err)
+        _check_refined(prm, gu, gv, ou, ov, seq.U, seq.V, seq.Um, seq.Vm, d[0], (k, w, h))
         epe = float(np.mean(np.hypot(gu - d[2], gv - d[3])))
         assert epe < 3.0, (k, w, h, epe)
 
@@ -199,5 +219,5 @@ def test_cfg3_crop_1920x256_u49_n512():
     pattern = prm.make_pattern(20261203)
     f1, f2, _, _ = synth.make_pair(303, 1920, 256, vmax=24.0)
     eng = _engine(prm, pattern)
-    assert _compare_sequence(eng, prm, pattern, [f1, f2], tol=FLOW_TOL_8836_TAPS) == 1
+    assert _compare_sequence(eng, prm, pattern, [f1, f2]) == 1
     eng.clean()

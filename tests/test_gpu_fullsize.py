@@ -24,6 +24,7 @@ import pytest
 
 import briefmatch_gb300 as bm
 import oracle
+from bmtest import trilateral_f64
 
 pytestmark = pytest.mark.gpu
 
@@ -139,35 +140,7 @@ def test_full_size_pair(W, H, u, N, vmax):
     err = max(np.abs(out[0, r0:r0 + rr] - Uo[margin:margin + rr]).max(),
               np.abs(out[1, r0:r0 + rr] - Vo[margin:margin + rr]).max())
     assert err <= (FLOW_TOL if s <= 24 else 3 * FLOW_TOL), err
-    ex_u, ex_v = _trilateral_f64(U, V, med[0], med[1], f0, r0, rr, s, prm.sEPE, prm.sI, prm.sS)
+    ex_u, ex_v = trilateral_f64(U, V, med[0], med[1], f0, r0, rr, s, prm.sEPE, prm.sI, prm.sS)
     err64 = max(np.abs(out[0, r0:r0 + rr] - ex_u).max(), np.abs(out[1, r0:r0 + rr] - ex_v).max())
     assert err64 <= FLOW_TOL, err64
     eng.clean()
-
-
-def _trilateral_f64(U, V, Um, Vm, I, r0, rows, s, sEPE, sI, sS):
-    """The cross-trilateral filter (briefmatch_cuda.cu:248-297: clamp-to-edge window
-    [-s, s)^2, weights exp(-EPE^2/2sEPE^2) exp(-dI^2/2sI^2) exp(-d^2/2sS^2) with
-    intensities / 255, weight sum floored at 1e-5) in float64, rows r0..r0+rows."""
-    H, W = U.shape
-    js, is_ = np.mgrid[-s:s, -s:s]
-    sp = (is_ ** 2 + js ** 2) / (2.0 * sS * sS)
-    outu = np.empty((rows, W))
-    outv = np.empty((rows, W))
-    for r in range(rows):
-        y = r0 + r
-        ys = np.clip(y + js, 0, H - 1)
-        for x0 in range(0, W, 128):
-            xs_c = np.arange(x0, min(W, x0 + 128))
-            xs = np.clip(xs_c[:, None, None] + is_[None], 0, W - 1)
-            yy = np.broadcast_to(ys[None], xs.shape)
-            u1 = U[yy, xs].astype(np.float64)
-            v1 = V[yy, xs].astype(np.float64)
-            du = u1 - Um[y, xs_c][:, None, None]
-            dv = v1 - Vm[y, xs_c][:, None, None]
-            dI = (I[yy, xs].astype(np.float64) - I[y, xs_c].astype(np.float64)[:, None, None]) / 255.0
-            w = np.exp(-(du * du + dv * dv) / (2.0 * sEPE * sEPE) - dI * dI / (2.0 * sI * sI) - sp[None])
-            Wt = np.maximum(w.sum(axis=(1, 2)), 1e-5)
-            outu[r, xs_c] = (w * u1).sum(axis=(1, 2)) / Wt
-            outv[r, xs_c] = (w * v1).sum(axis=(1, 2)) / Wt
-    return outu, outv
