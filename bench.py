@@ -553,8 +553,16 @@ def run_engine(args, torch, world, rank):
                                 % (head["ms_per_step_profiled"], head["ms_per_step"]))
     # the other large kernels' rooflines beside the dominant one
     roofline["others"] = [roofline_entry(torch, k, c, t, total_k, prm, head["clocks"]) for k, (c, t) in ranked[1:4]]
-    kernels = {k: {"launches": c, "ms": round(t, 4), "share": round(t / total_k, 4)} for k, (c, t) in
-               sorted(kstats.items(), key=lambda kv: -kv[1][1])}
+    def kernel_table(stats):
+        """Per kernel: launches and device ms over the K profiled steps, share of the
+        kernel time, and ms per pair (the stage costs of the engine)."""
+        tot = sum(t for _, t in stats.values())
+        return {k: {"launches": c, "ms": round(t, 4), "share": round(t / tot, 4),
+                    "ms_per_pair": round(t / (args.steps * PAIRS), 5)}
+                for k, (c, t) in sorted(stats.items(), key=lambda kv: -kv[1][1])}
+
+    kernels = kernel_table(kstats)
+    kernels_plain = kernel_table(rp["kstats"]) if head_name != "plain" else None
 
     batched = None
     if batch_inputs is not None:
@@ -613,6 +621,7 @@ def run_engine(args, torch, world, rank):
         "reference_cuda_build": ref_cuda,
         "learned": learned,
         "kernels": kernels,
+        "kernels_plain": kernels_plain,
         "batched": batched,
     }
     if rank == 0:

@@ -9,17 +9,25 @@
 // Every layer is a 3x3 convolution; the dilated middle layers widen the receptive
 // field to 63 cells (252 pixels) at the same cost per layer.
 //
-// Weights and activations are BF16, accumulation FP32, on the tensor cores through
-// mma.sync m16n8k16 implicit-GEMM kernels: forward, backward-data (the forward kernel
-// on the output gradient with flipped, transposed weights) and backward-weights
-// (pixels as the reduction dimension).  Activations are NHWC with the channel count
-// padded to a multiple of 16 (32-byte rows).  Training keeps FP32 master weights and
-// Adam moments; every step repacks the BF16 copies the kernels read.
+// Weights and activations are BF16, accumulation FP32, on the tensor cores.  The
+// forward pass of every layer and the backward-data pass of the 32-channel layers run
+// on the fifth-generation tensor cores (k_conv_umma): per CTA 128 cells of one image
+// row are the GEMM's M, the nine taps' 32 input channels its K (two K=16 steps per
+// tap), the output channels its N; TMA brings each tap's 128x32 activation tile and
+// the weights into shared memory in the 64-byte-swizzled K-major layout the MMA
+// reads, tcgen05.mma accumulates in tensor memory and tcgen05.ld hands each thread
+// its cell's channels for the epilogue.  The mma.sync m16n8k16 kernels (k_conv) stay
+// for the backward-data pass of the head (16 gradient channels), as the alternative
+// forward path (bm_net_set_umma), and the weight gradients (k_conv_wgrad: pixels as
+// the reduction dimension).  Activations are NHWC with the channel count padded to a
+// multiple of 16 (32-byte rows).  Training keeps FP32 master weights and Adam
+// moments; every step repacks the BF16 copies the kernels read.
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <vector>
 
+#include <cuda.h>  // CUtensorMap and its enums; the encoder is fetched through the runtime
 #include <cuda_bf16.h>
 
 #include "bm_internal.h"
@@ -30,7 +38,7 @@ constexpr int NL = 6;                               // layers
 constexpr int CIN_R[NL] = {32, 32, 32, 32, 32, 32};  // real input channels
 constexpr int COUT_R[NL] = {32, 32, 32, 32, 32, 3};
 constexpr int CIN_P[NL] = {32, 32, 32, 32, 32, 32};  // padded (multiple of 16)
-constexpr int COUT_P[NL] = {32, 32, 32, 32, 32, 8};  // padded (multiple of 8)
+constexpr int COUT_P[NL] = {32, 32, 32, 32, 32, 16};  // padded (multiple of 16: the head is N=16 on tcgen05)
 constexpr int DIL[NL] = {1, 2, 4, 8, 1, 1};          // dilation of each layer's 3x3 taps
 constexpr int NIN = 32;                              // input channels: 16 pixels of each frame's 4x4 block
 
@@ -430,6 +438,286 @@ cudaError_t conv_wgrad(int l, const __nv_bfloat16* X, const __nv_bfloat16* dY, i
     }
 }
 
+// ---------------------------------------------------------------------------
+// tcgen05 implicit-GEMM 3x3 convolution.  One CTA of 128 threads per run of UM = 128
+// consecutive cells of one image row: D[cell][co] = sum over taps t and input channels
+// ci of X[cell + shift(t)][ci] * W[t][co][ci].  Shared memory holds the nine taps'
+// A tiles (128 cells x 32 channels, 8 KB each) and the weights B (9 x N x 32); both
+// arrive by TMA with 64-byte swizzling, which is the canonical K-major layout the MMA
+// descriptors name (rows of 64 bytes, 8-row groups 512 bytes apart).  A tap whose
+// source row lies outside the image is neither loaded nor multiplied (its A tile would
+// be zeros); a tap shifted past the left or right edge reads TMA's zero fill.  Thread 0
+// issues the copies and the 18 MMAs (M=128, N, K=16) into a 32-column TMEM
+// accumulator; all four warps then read their 32 TMEM lanes (cells) and apply the
+// epilogue.  Every wait is bounded: a wait that gives up records an error word and the
+// CTA still frees its tensor memory before it returns.
+// ---------------------------------------------------------------------------
+constexpr int UM = 128;                                 // cells per CTA (MMA M)
+constexpr uint32_t U_TAP_A = UM * 32 * 2;               // bytes of one tap's A tile
+constexpr unsigned long long U_POLLS = 1ull << 20;      // polls of a wait before it gives up
+
+constexpr size_t umma_smem(int n) { return 1024 + 9 * (size_t)U_TAP_A + 9 * (size_t)n * 64; }
+
+__device__ __forceinline__ uint32_t s_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(s_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(s_addr(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(s_addr(bar)) : "memory");
+}
+// Polls the barrier's phase `parity` at most `polls` times; true once it completed.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, unsigned long long polls)
+{
+    for (unsigned long long i = 0; i < polls; i++) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(s_addr(bar)), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (i > 64) __nanosleep(64);
+    }
+    return false;
+}
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int c0, int c1, int c2, uint64_t* bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+        ::"r"(s_addr(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(s_addr(bar))
+        : "memory");
+}
+// Shared-memory matrix descriptor: K-major, 64-byte swizzle, 8-row groups 512 B apart.
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFF);       // start address
+    d |= (uint64_t)1 << 16;                       // leading byte offset (unused for swizzled K-major)
+    d |= (uint64_t)(512 >> 4) << 32;              // stride byte offset: next 8-row group
+    d |= (uint64_t)1 << 46;                       // descriptor version (sm_100 family)
+    d |= (uint64_t)4 << 61;                       // swizzle mode: 64-byte
+    return d;
+}
+// Instruction descriptor of kind::f16: BF16 A and B (K-major), FP32 D, M x N.
+__host__ __device__ constexpr uint32_t umma_idesc(int m, int n)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+template <int EPI, int N>
+__global__ void __launch_bounds__(128) k_conv_umma(const __grid_constant__ CUtensorMap tmX,
+                                                   const __grid_constant__ CUtensorMap tmW,
+                                                   const float* __restrict__ bias,
+                                                   const __nv_bfloat16* __restrict__ act, void* __restrict__ out,
+                                                   int h, int w, int dil, int cout_real, int out_stride,
+                                                   int* __restrict__ err)
+{
+    static_assert(N == 16 || N == 32, "N is 16 or 32 output channels");
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+    unsigned char* sA = sm;                     // 9 taps x 8 KB
+    unsigned char* sB = sm + 9 * U_TAP_A;       // 9 taps x N rows x 64 B
+    __shared__ __align__(8) uint64_t bar_load, bar_mma;
+    __shared__ uint32_t s_tmem;
+    __shared__ int s_ok;
+
+    const int tiles_x = (w + UM - 1) / UM;
+    const int row = blockIdx.x / tiles_x;               // image row over the batch, b * h + y
+    const int x0 = (blockIdx.x - row * tiles_x) * UM;
+    const int y = row % h;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    if (threadIdx.x == 0) {
+        mbar_init(&bar_load, 1);
+        mbar_init(&bar_mma, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        s_ok = 1;
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 32;" ::"r"(s_addr(&s_tmem))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = s_tmem;
+
+    if (threadIdx.x == 0) {
+        uint32_t taps = 0, bytes = 9u * N * 64;
+        for (int t = 0; t < 9; t++) {
+            const int r = y + (t / 3 - 1) * dil;
+            if (r >= 0 && r < h) {
+                taps |= 1u << t;
+                bytes += U_TAP_A;
+            }
+        }
+        mbar_expect_tx(&bar_load, bytes);
+        tma_load_3d(sB, &tmW, 0, 0, 0, &bar_load);
+        for (int t = 0; t < 9; t++)
+            if (taps >> t & 1u)
+                tma_load_3d(sA + t * U_TAP_A, &tmX, 0, x0 + (t % 3 - 1) * dil, row + (t / 3 - 1) * dil, &bar_load);
+        if (mbar_wait(&bar_load, 0, U_POLLS)) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            constexpr uint32_t idesc = umma_idesc(UM, N);
+            uint32_t acc = 0;
+            for (int t = 0; t < 9; t++) {
+                if (!(taps >> t & 1u)) continue;
+                const uint32_t a0 = s_addr(sA + t * U_TAP_A), b0 = s_addr(sB + t * N * 64);
+#pragma unroll
+                for (int kh = 0; kh < 2; kh++) {  // K = 16 channels (32 bytes) per MMA
+                    const uint64_t ad = umma_desc(a0 + kh * 32), bd = umma_desc(b0 + kh * 32);
+                    asm volatile(
+                        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+                        ::"r"(tmem), "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+                        : "memory");
+                    acc = 1;
+                }
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                         ::"r"(s_addr(&bar_mma)) : "memory");
+        } else {
+            // the copies did not land in time: give them one more bounded wait (they
+            // write this CTA's shared memory) and release the others without an MMA
+            atomicExch(err, 1);
+            s_ok = 0;
+            mbar_wait(&bar_load, 0, U_POLLS);
+            mbar_arrive(&bar_mma);
+        }
+    }
+    const bool done = mbar_wait(&bar_mma, 0, U_POLLS);
+    if (!done) atomicExch(err, 2);
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (done && s_ok) {
+        uint32_t r[N];
+        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+        if constexpr (N == 32) {
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                  "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                  "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
+                  "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
+                  "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+                : "r"(taddr));
+        } else {
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                "[%16];"
+                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                  "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                  "=r"(r[15])
+                : "r"(taddr));
+        }
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        const int x = x0 + warp * 32 + lane;
+        if (x < w) {
+            const size_t pix = (size_t)row * w + x;
+            if constexpr (EPI == EPI_LINEAR_F32) {
+                float* o = reinterpret_cast<float*>(out) + pix * out_stride;
+#pragma unroll
+                for (int co = 0; co < N; co++)
+                    if (co < cout_real) o[co] = __uint_as_float(r[co]) + __ldg(bias + co);
+            } else {
+                uint32_t packed[N / 2];
+                if constexpr (EPI == EPI_MASK_BF16) {
+                    const uint4* m4 = reinterpret_cast<const uint4*>(act + pix * out_stride);
+#pragma unroll
+                    for (int q = 0; q < N / 8; q++) {
+                        const uint4 mv = m4[q];
+                        const uint32_t mw[4] = {mv.x, mv.y, mv.z, mv.w};
+#pragma unroll
+                        for (int k = 0; k < 4; k++) {
+                            const int co = q * 8 + 2 * k;
+                            const __nv_bfloat162 m = *reinterpret_cast<const __nv_bfloat162*>(&mw[k]);
+                            const float v0 = __bfloat162float(m.x) > 0.0f ? __uint_as_float(r[co]) : 0.0f;
+                            const float v1 = __bfloat162float(m.y) > 0.0f ? __uint_as_float(r[co + 1]) : 0.0f;
+                            packed[co / 2] = pack_bf16(v0, v1);
+                        }
+                    }
+                } else {
+#pragma unroll
+                    for (int co = 0; co < N; co += 2)
+                        packed[co / 2] = pack_bf16(fmaxf(__uint_as_float(r[co]) + __ldg(bias + co), 0.0f),
+                                                   fmaxf(__uint_as_float(r[co + 1]) + __ldg(bias + co + 1), 0.0f));
+                }
+                uint4* o4 = reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(out) + pix * out_stride);
+#pragma unroll
+                for (int q = 0; q < N / 8; q++)
+                    o4[q] = make_uint4(packed[4 * q], packed[4 * q + 1], packed[4 * q + 2], packed[4 * q + 3]);
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 32;" ::"r"(tmem) : "memory");
+}
+
+// cuTensorMapEncodeTiled, fetched through the runtime (the library does not link the
+// driver library itself).
+typedef CUresult (*EncodeTiled)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiled encoder()
+{
+    static EncodeTiled fn = nullptr;
+    static bool looked_up = false;
+    if (!looked_up) {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiled>(f);
+        looked_up = true;
+    }
+    return fn;
+}
+
+// A 3-D BF16 tensor map with 64-byte rows: dims {32 channels, d1, d2}, box {32, b1, b2},
+// 64-byte swizzle, zero fill out of bounds.
+bool encode_map(CUtensorMap* map, const void* base, uint64_t d1, uint64_t d2, uint32_t b1, uint32_t b2)
+{
+    EncodeTiled enc = encoder();
+    if (!enc) return false;
+    const cuuint64_t dims[3] = {32, d1, d2};
+    const cuuint64_t strides[2] = {64, 64 * d1};
+    const cuuint32_t box[3] = {32, b1, b2};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// Activations [B*h][w][32] as the A operand of a conv layer.
+bool act_map(CUtensorMap* map, const __nv_bfloat16* X, int B, int h, int w)
+{
+    return encode_map(map, X, (uint64_t)w, (uint64_t)B * h, UM, 1);
+}
+// Weights [9][n][32] as the B operand (all nine taps in one copy).
+bool weight_map(CUtensorMap* map, const __nv_bfloat16* W, int n) { return encode_map(map, W, (uint64_t)n, 9, n, 9); }
+
+template <int EPI, int N>
+cudaError_t launch_conv_umma(const CUtensorMap& mx, const CUtensorMap& mw, const float* bias, const __nv_bfloat16* act,
+                             void* out, int B, int h, int w, int dil, int cout_real, int out_stride, int* err,
+                             cudaStream_t st)
+{
+    const unsigned tiles = (unsigned)(((w + UM - 1) / UM) * (size_t)B * h);
+    k_conv_umma<EPI, N><<<tiles, 128, umma_smem(N), st>>>(mx, mw, bias, act, out, h, w, dil, cout_real, out_stride,
+                                                           err);
+    return cudaGetLastError();
+}
+
 // Dynamic shared-memory opt-in of every instantiation above 48 KB (once per process
 // and device; called from bm_net_create, outside any stream capture).
 cudaError_t conv_smem_optin()
@@ -449,6 +737,9 @@ cudaError_t conv_smem_optin()
         set((const void*)k_conv<32, 32, EPI_MASK_BF16, 8>, conv_smem(32, 32, 8)),
         set((const void*)k_conv_wgrad<32, 32, 4>, wgrad_smem(32, 32, 4)),
         set((const void*)k_conv_wgrad<32, 32, 8>, wgrad_smem(32, 32, 8)),
+        set((const void*)k_conv_umma<EPI_RELU_BF16, 32>, umma_smem(32)),
+        set((const void*)k_conv_umma<EPI_MASK_BF16, 32>, umma_smem(32)),
+        set((const void*)k_conv_umma<EPI_LINEAR_F32, 16>, umma_smem(16)),
     };
     for (cudaError_t x : es)
         if (x != cudaSuccess) return x;
@@ -478,6 +769,17 @@ struct bm_net {
     float* d_loss = nullptr;            // 3 floats
     uint64_t step = 0;
     bool packed = false;
+
+    // tcgen05 path (k_conv_umma): tensor maps of the weights (fixed buffers) and of the
+    // activations for the last (B, h, w) seen; error word of its bounded waits
+    bool umma = false;
+    int* d_err = nullptr;
+    CUtensorMap map_wf[NL];
+    CUtensorMap map_wb[NL];
+    uint32_t map_B = 0, map_h = 0, map_w = 0;
+    CUtensorMap map_in;
+    CUtensorMap map_act[NL - 1];
+    CUtensorMap map_dy[2];
 };
 
 namespace {
@@ -518,6 +820,21 @@ bm_status check_dims(bm_net* n, uint32_t B, uint32_t h, uint32_t w)
     return BM_OK;
 }
 
+// Tensor maps of the activation buffers for a (B, h, w) call (host-side encoding only).
+bool ensure_act_maps(bm_net* n, uint32_t B, uint32_t h, uint32_t w)
+{
+    if (n->map_B == B && n->map_h == h && n->map_w == w) return true;
+    const int Bi = (int)B, hi = (int)h, wi = (int)w;
+    bool ok = act_map(&n->map_in, n->d_in, Bi, hi, wi);
+    for (int l = 0; ok && l < NL - 1; l++) ok = act_map(&n->map_act[l], n->d_act[l], Bi, hi, wi);
+    for (int k = 0; ok && k < 2; k++) ok = act_map(&n->map_dy[k], n->d_dy[k], Bi, hi, wi);
+    if (!ok) return false;
+    n->map_B = B;
+    n->map_h = h;
+    n->map_w = w;
+    return true;
+}
+
 bm_status forward(bm_net* n, uint32_t B, uint32_t h, uint32_t w, cudaStream_t st)
 {
     if (!n->packed) {
@@ -525,10 +842,21 @@ bm_status forward(bm_net* n, uint32_t B, uint32_t h, uint32_t w, cudaStream_t st
         if (s != BM_OK) return s;
     }
     const int Bi = (int)B, hi = (int)h, wi = (int)w;
+    if (n->umma) {
+        if (!ensure_act_maps(n, B, h, w)) return nfail(BM_ERR_CUDA, "bm_net: tensor map encoding failed");
+        for (int l = 0; l <= 4; l++)
+            BN_CUDA((launch_conv_umma<EPI_RELU_BF16, 32>(l == 0 ? n->map_in : n->map_act[l - 1], n->map_wf[l],
+                                                          n->d_master + n->poff[l] + layer_w_count(l), nullptr,
+                                                          n->d_act[l], Bi, hi, wi, DIL[l], 32, 32, n->d_err, st)));
+        BN_CUDA((launch_conv_umma<EPI_LINEAR_F32, 16>(n->map_act[4], n->map_wf[5],
+                                                       n->d_master + n->poff[5] + layer_w_count(5), nullptr, n->d_out,
+                                                       Bi, hi, wi, DIL[5], 3, 3, n->d_err, st)));
+        return BM_OK;
+    }
     for (int l = 0; l <= 4; l++)
         BN_CUDA(conv_fwd(l, l == 0 ? n->d_in : n->d_act[l - 1], n->d_wf[l], n->d_master + n->poff[l] + layer_w_count(l),
                          n->d_act[l], Bi, hi, wi, st));
-    BN_CUDA((launch_conv<32, 8, EPI_LINEAR_F32, 1>(n->d_act[4], n->d_wf[5], n->d_master + n->poff[5] + layer_w_count(5),
+    BN_CUDA((launch_conv<32, 16, EPI_LINEAR_F32, 1>(n->d_act[4], n->d_wf[5], n->d_master + n->poff[5] + layer_w_count(5),
                                                    nullptr, n->d_out, Bi, hi, wi, 3, 3, st)));
     return BM_OK;
 }
@@ -573,10 +901,16 @@ bm_status bm_net_create(uint32_t max_batch, uint32_t max_h4, uint32_t max_w4, bm
         ok = bmk::device_malloc((void**)&n->d_wf[l], (size_t)9 * COUT_P[l] * CIN_P[l] * 2) == cudaSuccess &&
              bmk::device_malloc((void**)&n->d_wb[l], (size_t)9 * CIN_P[l] * coutp16 * 2) == cudaSuccess;
     }
+    if (ok) ok = bmk::device_malloc((void**)&n->d_err, sizeof(int)) == cudaSuccess;
     if (!ok) {
         bm_net_destroy(n);
         return nfail(BM_ERR_NOMEM, "bm_net_create: device allocation failed");
     }
+    cudaMemset(n->d_err, 0, sizeof(int));
+    // the tcgen05 path, when the driver encodes the weights' tensor maps
+    n->umma = true;
+    for (int l = 0; n->umma && l < NL; l++) n->umma = weight_map(&n->map_wf[l], n->d_wf[l], COUT_P[l]);
+    for (int l = 1; n->umma && l < NL - 1; l++) n->umma = weight_map(&n->map_wb[l], n->d_wb[l], CIN_P[l]);
     cudaMemset(n->d_m, 0, off * 4);
     cudaMemset(n->d_v, 0, off * 4);
     cudaMemset(n->d_dy[0], 0, px * 32 * 2);
@@ -606,7 +940,8 @@ bm_status bm_net_create(uint32_t max_batch, uint32_t max_h4, uint32_t max_w4, bm
 bm_status bm_net_destroy(bm_net* n)
 {
     if (!n) return BM_OK;
-    void* ptrs[] = {n->d_master, n->d_grad, n->d_m, n->d_v, n->d_in, n->d_out, n->d_loss, n->d_dy[0], n->d_dy[1]};
+    void* ptrs[] = {n->d_master, n->d_grad, n->d_m, n->d_v, n->d_in, n->d_out, n->d_loss, n->d_dy[0], n->d_dy[1],
+                    n->d_err};
     for (void* q : ptrs)
         if (q) bmk::device_free(q);
     for (int l = 0; l < NL; l++) {
@@ -662,6 +997,39 @@ bm_status bm_net_set_input(bm_net* n, const uint16_t* d_in, uint32_t B, uint32_t
     return BM_OK;
 }
 
+bm_status bm_net_set_umma(bm_net* n, int on)
+{
+    if (!n) return nfail(BM_ERR_INVALID, "bm_net_set_umma: null");
+    if (!on) {
+        n->umma = false;
+        return BM_OK;
+    }
+    bool ok = true;
+    for (int l = 0; ok && l < NL; l++) ok = weight_map(&n->map_wf[l], n->d_wf[l], COUT_P[l]);
+    for (int l = 1; ok && l < NL - 1; l++) ok = weight_map(&n->map_wb[l], n->d_wb[l], CIN_P[l]);
+    if (!ok) return nfail(BM_ERR_CUDA, "bm_net_set_umma: tensor map encoding unavailable");
+    n->umma = true;
+    n->map_B = n->map_h = n->map_w = 0;
+    return BM_OK;
+}
+
+int bm_net_umma(const bm_net* n) { return n && n->umma ? 1 : 0; }
+
+bm_status bm_net_check(bm_net* n, void* stream)
+{
+    if (!n) return nfail(BM_ERR_INVALID, "bm_net_check: null");
+    int h = 0;
+    BN_CUDA(cudaMemcpyAsync(&h, n->d_err, sizeof(int), cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+    BN_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+    if (h) {
+        BN_CUDA(cudaMemsetAsync(n->d_err, 0, sizeof(int), (cudaStream_t)stream));
+        BN_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+        return nfail(BM_ERR_TIMEOUT, h == 1 ? "bm_net: a tensor-core layer's copies did not arrive in time"
+                                            : "bm_net: a tensor-core layer's MMA did not complete in time");
+    }
+    return BM_OK;
+}
+
 bm_status bm_net_forward(bm_net* n, uint32_t B, uint32_t h, uint32_t w, float* d_out, void* stream)
 {
     if (!n) return nfail(BM_ERR_INVALID, "bm_net_forward: null");
@@ -704,7 +1072,11 @@ bm_status bm_net_train_step(bm_net* n, uint32_t B, uint32_t h, uint32_t w, const
     for (int l = 4; l >= 1; l--) {
         BN_CUDA(conv_wgrad(l, n->d_act[l - 1], n->d_dy[cur], Bi, hi, wi, g + n->poff[l], g + n->poff[l] + layer_w_count(l),
                            st));
-        BN_CUDA(conv_bwd_data(l, n->d_dy[cur], n->d_wb[l], n->d_act[l - 1], n->d_dy[cur ^ 1], Bi, hi, wi, st));
+        if (n->umma)
+            BN_CUDA((launch_conv_umma<EPI_MASK_BF16, 32>(n->map_dy[cur], n->map_wb[l], nullptr, n->d_act[l - 1],
+                                                          n->d_dy[cur ^ 1], Bi, hi, wi, DIL[l], 32, 32, n->d_err, st)));
+        else
+            BN_CUDA(conv_bwd_data(l, n->d_dy[cur], n->d_wb[l], n->d_act[l - 1], n->d_dy[cur ^ 1], Bi, hi, wi, st));
         cur ^= 1;
     }
     BN_CUDA(conv_wgrad(0, n->d_in, n->d_dy[cur], Bi, hi, wi, g + n->poff[0], g + n->poff[0] + layer_w_count(0), st));

@@ -32,6 +32,9 @@ def _declare():
         "bm_net_forward": (c.c_int, [c.c_void_p, c.c_uint32, c.c_uint32, c.c_uint32, c.c_void_p, c.c_void_p]),
         "bm_net_train_step": (c.c_int, [c.c_void_p, c.c_uint32, c.c_uint32, c.c_uint32, c.c_void_p, c.c_float,
                                         c.c_void_p, c.c_void_p, c.c_void_p]),
+        "bm_net_set_umma": (c.c_int, [c.c_void_p, c.c_int]),
+        "bm_net_umma": (c.c_int, [c.c_void_p]),
+        "bm_net_check": (c.c_int, [c.c_void_p, c.c_void_p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -100,6 +103,18 @@ class ProposalNet:
 
     def forward(self, B, h, w, d_out=0, stream=0):
         check(lib().bm_net_forward(self._n, B, h, w, ctypes.c_void_p(d_out), ctypes.c_void_p(stream)))
+
+    def set_umma(self, on=True):
+        """tcgen05 (on) or mma.sync (off) convolutions; see bm_net_set_umma."""
+        check(lib().bm_net_set_umma(self._n, int(bool(on))))
+
+    @property
+    def umma(self):
+        return bool(lib().bm_net_umma(self._n))
+
+    def check(self, stream=0):
+        """Raises if a tensor-core layer's bounded wait gave up (bm_net_check)."""
+        check(lib().bm_net_check(self._n, ctypes.c_void_p(stream)))
 
     def train_step(self, B, h, w, d_target, lr, d_grad=0, stream=0):
         loss = np.zeros(3, np.float32)

@@ -330,6 +330,16 @@ bm_status bm_net_forward(bm_net* n, uint32_t B, uint32_t h, uint32_t w, float* d
  * h_loss (may be NULL) receives (flow loss, confidence loss, confident fraction). */
 bm_status bm_net_train_step(bm_net* n, uint32_t B, uint32_t h, uint32_t w, const float* d_target, float lr,
                             float* d_grad_out, float* h_loss, void* stream);
+/* Which tensor-core path the convolutions take: on (the default where the driver
+ * encodes tensor maps) the forward pass of every layer and the backward-data pass of
+ * the 32-channel layers run as tcgen05 MMAs into tensor memory fed by TMA; off, as
+ * mma.sync m16n8k16 kernels.  Both give the same network up to FP32 summation order. */
+bm_status bm_net_set_umma(bm_net* n, int on);
+int bm_net_umma(const bm_net* n);
+/* Synchronises `stream` and reports BM_ERR_TIMEOUT if a tensor-core layer's bounded
+ * wait for its copies or its MMAs gave up since the last check (its outputs are then
+ * undefined); clears the record. */
+bm_status bm_net_check(bm_net* n, void* stream);
 
 /* Attach a proposal network to a context (NULL detaches).  Every later bm_frame that
  * matches a pair runs the network on the previous and current frames and initialises

@@ -1,5 +1,7 @@
 """The proposal network's tensor-core kernels against the FP32 CPU restatement
-(oracle/net_oracle.py): forward output, loss terms and every layer's gradient."""
+(oracle/net_oracle.py): forward output, loss terms and every layer's gradient, on
+both tensor-core paths (tcgen05 MMAs into tensor memory, the default, and mma.sync);
+the two paths against each other on images wider than one 128-cell MMA tile."""
 from __future__ import annotations
 
 import numpy as np
@@ -80,21 +82,32 @@ def test_input_preparation():
     assert np.array_equal(o[..., 0], want_u) and np.array_equal(o[..., 1], want_v)
 
 
-def test_forward_matches_oracle():
+def test_tcgen05_path_is_the_default():
+    net = ProposalNet(1, 8, 8)
+    assert net.umma
+    net.close()
+
+
+@pytest.mark.parametrize("umma", [True, False])
+def test_forward_matches_oracle(umma):
     B, h, w = 2, 20, 36
     net, p, x, _ = _setup(B, h, w)
+    net.set_umma(umma)
     out = torch.empty(B, h, w, 3, device="cuda")
     net.forward(B, h, w, out.data_ptr())
     torch.cuda.synchronize()
     got = out.cpu().numpy()
+    net.check()
     want, _ = net_oracle.forward(p, x)
     err = np.abs(got - want).max() / max(1e-6, np.abs(want).max())
     assert err < 2e-2, err
 
 
-def test_gradients_match_oracle():
+@pytest.mark.parametrize("umma", [True, False])
+def test_gradients_match_oracle(umma):
     B, h, w = 2, 20, 36
     net, p, x, tgt = _setup(B, h, w, seed=1)
+    net.set_umma(umma)
     d_t = torch.from_numpy(tgt).cuda()
     d_g = torch.empty(param_count(), device="cuda")
     loss = net.train_step(B, h, w, d_t.data_ptr(), 0.0, d_g.data_ptr())
@@ -121,3 +134,28 @@ def test_training_reduces_loss():
     for _ in range(60):
         last = net.train_step(B, h, w, d_t.data_ptr(), 1e-3)
     assert last[0] < 0.8 * first[0]
+
+
+@pytest.mark.parametrize("B,h,w", [(1, 109, 256), (2, 7, 300), (3, 5, 17)])
+def test_tcgen05_equals_mma_sync(B, h, w):
+    """Whole 128-cell tiles, a ragged last tile and an image narrower than one tile:
+    the tcgen05 forward and training step equal the mma.sync ones up to FP32 summation
+    order (both round activations to BF16 between layers)."""
+    net, p, x, tgt = _setup(B, h, w, seed=3)
+    d_t = torch.from_numpy(tgt).cuda()
+    outs, grads = [], []
+    for umma in (True, False):
+        net.set_umma(umma)
+        out = torch.empty(B, h, w, 3, device="cuda")
+        net.forward(B, h, w, out.data_ptr())
+        g = torch.empty(param_count(), device="cuda")
+        net.train_step(B, h, w, d_t.data_ptr(), 0.0, g.data_ptr())
+        torch.cuda.synchronize()
+        net.check()
+        outs.append(out.cpu().numpy())
+        grads.append(g.cpu().numpy())
+    scale = max(1e-6, float(np.abs(outs[1]).max()))
+    assert float(np.abs(outs[0] - outs[1]).max()) / scale < 1e-2
+    rel = np.linalg.norm(grads[0] - grads[1]) / max(1e-12, np.linalg.norm(grads[1]))
+    assert rel < 2e-2, rel
+    net.close()
