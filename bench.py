@@ -489,6 +489,7 @@ def net_forward_timing(torch, net, d_frames, stream, reps=50):
     ms = e0.elapsed_time(e1) / reps
     flops = flops_per_pixel() * h4 * w4
     return {"ms_per_pair": ms, "gflop_per_pair": flops / 1e9, "tflop_s": flops / (ms * 1e-3) / 1e12,
+            "path": {2: "tcgen05, one cooperative launch", 1: "tcgen05, a launch per layer", 0: "mma.sync"}[net.umma],
             "note": "input preparation + 6 conv layers, 1 pair, back to back"}
 
 
@@ -524,8 +525,15 @@ def run_engine(args, torch, world, rank):
             sch, table = (sch + (0,))[:3], "given on the command line"
         else:
             sch, table = choose_schedule(torch, prm, pattern, net, stream)
+        # the network's forward on both tensor-core paths (tcgen05 is the engine's)
+        nf = {}
+        for path, mode in (("mma_sync", 0), ("tcgen05_per_layer", 1), ("tcgen05_fused", 2)):
+            net.set_umma(mode)
+            nf[path] = net_forward_timing(torch, net, d_frames, stream)
+        net.check(stream.cuda_stream)
+        nf["tcgen05_fused"]["ctas"] = net.fused_ctas
         learned = {"weights": os.path.relpath(learn.DEFAULT_WEIGHTS, ROOT), "confidence": PROPOSAL_CONF,
-                   "calibration": table, "schedule": None, "net_forward": net_forward_timing(torch, net, d_frames, stream)}
+                   "calibration": table, "schedule": None, "net_forward": nf}
         if sch is not None:
             seng = open_engine(torch, prm, pattern, stream, net, sch)
             rl = measure(args, torch, world, seng, d_frames, flows, stream, flush)

@@ -19,9 +19,10 @@ namespace bmk {
 namespace {
 
 // The colour wheel, colorcode.cpp:27-50: integer channel values from integer
-// divisions, 15 + 6 + 4 + 11 + 13 + 6 = 55 entries (r, g, b).
+// divisions, 15 + 6 + 4 + 11 + 13 + 6 = 55 entries (r, g, b), kept as the floats
+// computeColor forms from them (value / 255.0, rounded once).
 struct Wheel {
-    unsigned char c[55][3];
+    float f[55][3];  // colorwheel[k][b] / 255.0 rounded to float (colorcode.cpp:64-65)
 };
 
 Wheel make_wheel()
@@ -30,9 +31,9 @@ Wheel make_wheel()
     Wheel w;
     int k = 0;
     auto set = [&](int r, int g, int b) {
-        w.c[k][0] = (unsigned char)r;
-        w.c[k][1] = (unsigned char)g;
-        w.c[k][2] = (unsigned char)b;
+        w.f[k][0] = (float)(r / 255.0);
+        w.f[k][1] = (float)(g / 255.0);
+        w.f[k][2] = (float)(b / 255.0);
         k++;
     };
     for (int i = 0; i < RY; i++) set(255, 255 * i / RY, 0);
@@ -101,15 +102,15 @@ __global__ void __launch_bounds__(256) k_flow_color(const float* __restrict__ U,
     const float at = __double2float_rn(atan2(-(double)fy, -(double)fx));  // correctly rounded float atan2
     const float a = __double2float_rn(__ddiv_rn((double)at, 3.14159265358979323846));
     const int ncols = 55;
-    const float fk = __double2float_rn(__dmul_rn(__ddiv_rn(__dadd_rn((double)a, 1.0), 2.0), (double)(ncols - 1)));
+    // (a + 1.0) / 2.0 * (ncols - 1); halving is exact, so it is a multiply by 0.5
+    const float fk = __double2float_rn(__dmul_rn(__dmul_rn(__dadd_rn((double)a, 1.0), 0.5), (double)(ncols - 1)));
     const int k0 = (int)fk;
     const int k1 = (k0 + 1) % ncols;
     const float f = __fsub_rn(fk, (float)k0);
     const float omf = __fsub_rn(1.0f, f);
 #pragma unroll
     for (int b = 0; b < 3; b++) {
-        const float col0 = __double2float_rn(__ddiv_rn((double)wheel.c[k0][b], 255.0));
-        const float col1 = __double2float_rn(__ddiv_rn((double)wheel.c[k1][b], 255.0));
+        const float col0 = wheel.f[k0][b], col1 = wheel.f[k1][b];
         float col = __fadd_rn(__fmul_rn(omf, col0), __fmul_rn(f, col1));
         if (rad <= 1.0f)
             col = __fsub_rn(1.0f, __fmul_rn(rad, __fsub_rn(1.0f, col)));  // saturation grows with radius

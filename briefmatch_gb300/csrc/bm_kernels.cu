@@ -12,6 +12,7 @@
 //   flow         uint32 per pixel, int16 nx in the low half, int16 ny in the high half
 //   cost         uint16 per pixel, the Hamming distance of the current candidate
 //                (the reference's D is cost/N)
+#include <climits>
 #include <mutex>
 
 #include "bm_device.cuh"
@@ -72,16 +73,62 @@ __global__ void __launch_bounds__(256) k_upsample(const T* __restrict__ in, floa
 // (syo + 2m) pixels at row pitch `pitch`; a pixel of the margin holds the value of
 // the nearest image pixel (each coordinate clamped), computed by the same Lanczos
 // expression, so every read of the margin equals a clamped read of the image.
-template <typename T>
-__global__ void __launch_bounds__(256) k_upsample_pad(const T* __restrict__ in, float* __restrict__ out, int pitch,
-                                                      int m, int sxi, int syi, int sxo, int syo,
-                                                      const float* __restrict__ lx, const int* __restrict__ ix,
-                                                      const float* __restrict__ ly, const int* __restrict__ iy)
+// Each thread computes UP_R output rows of one column (a block covers
+// TX x (TY * UP_R) outputs).  The rows share the column's six
+// weights and source columns, and rows whose Lanczos windows start on the same
+// source row share the products input * Lx: they are formed once per window (36
+// multiplies) and each output then takes its 36 multiply-adds onto them in the
+// reference's order (util_cuda.cu:140-152: over source columns, then rows;
+// v += (in * Lx) * Ly as one rounded product and an FMA, w += Lx * Ly as an FMA), so
+// every value equals upsample_val's bit for bit.
+constexpr int UP_R = 8;
+__global__ void __launch_bounds__(TX * TY) k_upsample_pad_rows(const uint8_t* __restrict__ in, float* __restrict__ out,
+                                                               int pitch, int m, int sxi, int syi, int sxo, int syo,
+                                                               const float* __restrict__ lx, const int* __restrict__ ix,
+                                                               const float* __restrict__ ly, const int* __restrict__ iy)
 {
-    const int X = blockIdx.x * TX + threadIdx.x, Y = blockIdx.y * TY + threadIdx.y;
-    if (X >= sxo + 2 * m || Y >= syo + 2 * m) return;
-    const int x = min(sxo - 1, max(0, X - m)), y = min(syo - 1, max(0, Y - m));
-    out[X + (size_t)Y * pitch] = upsample_val<T>(in, sxi, syi, lx, ix, ly, iy, x, y);
+    const int X = blockIdx.x * TX + threadIdx.x;
+    const int Y0 = (blockIdx.y * TY + threadIdx.y) * UP_R;
+    if (X >= sxo + 2 * m || Y0 >= syo + 2 * m) return;
+    const int x = min(sxo - 1, max(0, X - m));
+    float Lx[6];
+    int col[6];
+    const int x1 = __ldg(ix + x);
+#pragma unroll
+    for (int a = 0; a < 6; a++) {
+        Lx[a] = __ldg(lx + x * 6 + a);
+        col[a] = min(sxi - 1, max(0, x1 - 2 + a));
+    }
+    float P[6][6];  // P[a][b] = in[row b of the window][col a] * Lx[a]
+    int win = INT_MIN;
+#pragma unroll
+    for (int r = 0; r < UP_R; r++) {
+        const int Y = Y0 + r;
+        if (Y >= syo + 2 * m) break;
+        const int y = min(syo - 1, max(0, Y - m));
+        const int y1 = __ldg(iy + y);
+        if (y1 != win) {  // uniform across the warp (one output row per warp)
+            win = y1;
+#pragma unroll
+            for (int b = 0; b < 6; b++) {
+                const uint8_t* src = in + (size_t)min(syi - 1, max(0, y1 - 2 + b)) * sxi;
+#pragma unroll
+                for (int a = 0; a < 6; a++) P[a][b] = __fmul_rn((float)__ldg(src + col[a]), Lx[a]);
+            }
+        }
+        float Ly[6];
+#pragma unroll
+        for (int b = 0; b < 6; b++) Ly[b] = __ldg(ly + y * 6 + b);
+        float v = 0.0f, w = 0.0f;
+#pragma unroll
+        for (int a = 0; a < 6; a++)
+#pragma unroll
+            for (int b = 0; b < 6; b++) {
+                w = __fmaf_rn(Lx[a], Ly[b], w);
+                v = __fmaf_rn(P[a][b], Ly[b], v);
+            }
+        out[X + (size_t)Y * pitch] = v / w;
+    }
 }
 
 __global__ void k_u8_to_f32(const uint8_t* __restrict__ in, float* __restrict__ out, size_t n)
@@ -113,7 +160,7 @@ __global__ void __launch_bounds__(256) k_features(const float* __restrict__ I, u
     }
 }
 
-// BRIEF descriptors from an edge-replicated image (k_upsample_pad) whose margin is
+// BRIEF descriptors from an edge-replicated image (k_upsample_pad_rows) whose margin is
 // at least the pattern's largest offset: every pixel reads at the linear offsets
 // (no clamping, no border tiles); each thread computes feat_px<NSP>() pixels TX apart
 // (two up to 128-bit descriptors, where sharing each offset's address arithmetic
@@ -372,8 +419,8 @@ cudaError_t upsample_u8_pad(const uint8_t* in, float* out, int pitch, int m, int
                             const float* lx, const int* ix, const float* ly, const int* iy, cudaStream_t st)
 {
     if (m < 0 || pitch < sxo + 2 * m) return cudaErrorInvalidValue;
-    k_upsample_pad<uint8_t><<<grid2d(sxo + 2 * m, syo + 2 * m), dim3(TX, TY), 0, st>>>(in, out, pitch, m, sxi, syi, sxo,
-                                                                                       syo, lx, ix, ly, iy);
+    const dim3 g((sxo + 2 * m + TX - 1) / TX, (syo + 2 * m + TY * UP_R - 1) / (TY * UP_R));
+    k_upsample_pad_rows<<<g, dim3(TX, TY), 0, st>>>(in, out, pitch, m, sxi, syi, sxo, syo, lx, ix, ly, iy);
     return cudaGetLastError();
 }
 

@@ -22,6 +22,7 @@
 // the reduction dimension).  Activations are NHWC with the channel count padded to a
 // multiple of 16 (32-byte rows).  Training keeps FP32 master weights and Adam
 // moments; every step repacks the BF16 copies the kernels read.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -279,21 +280,31 @@ __global__ void k_net_input(const uint8_t* __restrict__ f0, const uint8_t* __res
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= w4 || y >= h4) return;
     uint32_t v[16];
+    // a cell's 4x4 block lies inside the frame (w4 = W / 4, h4 = H / 4); with W a
+    // multiple of 4 each of its rows is one aligned 32-bit word
+    const bool words = (W & 3) == 0 && (reinterpret_cast<uintptr_t>(f0) & 3) == 0 &&
+                       (reinterpret_cast<uintptr_t>(f1) & 3) == 0;
+    uint32_t row[2][4];
 #pragma unroll
     for (int f = 0; f < 2; f++) {
         const uint8_t* src = f ? f1 : f0;
 #pragma unroll
         for (int j = 0; j < 4; j++) {
-            const int yy = min(H - 1, y * 4 + j);
-#pragma unroll
-            for (int i = 0; i < 4; i += 2) {
-                const int xa = min(W - 1, x * 4 + i), xb = min(W - 1, x * 4 + i + 1);
-                const float a = src[(size_t)yy * W + xa] / 127.5f - 1.0f;
-                const float b = src[(size_t)yy * W + xb] / 127.5f - 1.0f;
-                v[f * 8 + j * 2 + i / 2] = pack_bf16(a, b);
-            }
+            const uint8_t* p = src + (size_t)(y * 4 + j) * W + x * 4;
+            row[f][j] = words ? __ldg(reinterpret_cast<const uint32_t*>(p))
+                              : (uint32_t)p[0] | ((uint32_t)p[1] << 8) | ((uint32_t)p[2] << 16) | ((uint32_t)p[3] << 24);
         }
     }
+#pragma unroll
+    for (int f = 0; f < 2; f++)
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+#pragma unroll
+            for (int i = 0; i < 4; i += 2) {
+                const float a = (float)((row[f][j] >> (8 * i)) & 0xFFu) / 127.5f - 1.0f;
+                const float b = (float)((row[f][j] >> (8 * (i + 1))) & 0xFFu) / 127.5f - 1.0f;
+                v[f * 8 + j * 2 + i / 2] = pack_bf16(a, b);
+            }
     uint4* o = reinterpret_cast<uint4*>(out + ((size_t)y * w4 + x) * NIN);
 #pragma unroll
     for (int q = 0; q < 4; q++) o[q] = make_uint4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
@@ -593,10 +604,11 @@ __global__ void __launch_bounds__(128) k_conv_umma(const __grid_constant__ CUten
             mbar_arrive(&bar_mma);
         }
     }
-    const bool done = mbar_wait(&bar_mma, 0, U_POLLS);
-    if (!done) atomicExch(err, 2);
+    // tcgen05.ld is warp-collective: the block agrees on one outcome of the wait
+    const bool mine = mbar_wait(&bar_mma, 0, U_POLLS);
+    const bool done = __syncthreads_and(mine ? 1 : 0) != 0;
+    if (!done && threadIdx.x == 0) atomicExch(err, 2);
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    __syncthreads();
     if (done && s_ok) {
         uint32_t r[N];
         const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
@@ -718,6 +730,235 @@ cudaError_t launch_conv_umma(const CUtensorMap& mx, const CUtensorMap& mw, const
     return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// The whole forward pass in one cooperative launch (k_net_fused): every CTA keeps
+// its tensor memory and barriers for all six layers and walks the layer's 128-cell
+// tiles with a grid stride; between layers the CTAs meet at a bounded grid barrier,
+// the outputs of a layer having been written with plain stores and fenced for the
+// next layer's TMA reads (proxy fences on both sides of the barrier).  It replaces
+// six launches and their per-launch set-up (barrier init, TMEM allocation, weight
+// copy) with one.
+// ---------------------------------------------------------------------------
+struct NetGridBar {
+    unsigned int arrived;
+    unsigned int generation;
+    unsigned int error;
+};
+
+struct NetFusedArgs {
+    CUtensorMap in_map[NL];    // A operand of each layer (layer 0: the input image)
+    CUtensorMap w_map[NL];     // B operand (weights) of each layer
+    const float* bias[NL];
+    __nv_bfloat16* act[NL - 1];  // outputs of layers 0..4
+    float* head;                 // [cells][3]
+    int h, w, rows;              // rows = B * h
+    int dil[NL];
+    unsigned long long polls;
+    NetGridBar* bar;
+    int* err;
+};
+
+// Bounded grid barrier: false when it gave up (then the error word is set).
+__device__ __forceinline__ bool net_grid_sync(NetGridBar* gb, unsigned int nblocks, unsigned long long polls)
+{
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        ok = 1;
+        volatile unsigned int* vgen = &gb->generation;
+        volatile unsigned int* verr = &gb->error;
+        const unsigned int gen = *vgen;
+        __threadfence();
+        if (atomicAdd(&gb->arrived, 1u) == nblocks - 1) {
+            atomicExch(&gb->arrived, 0u);
+            __threadfence();
+            atomicAdd(&gb->generation, 1u);
+        } else {
+            unsigned long long i = 0;
+            while (*vgen == gen) {
+                if (*verr || ++i > polls) {
+                    atomicExch(&gb->error, 1u);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(128);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+// Epilogue of one tile: TMEM lanes of this warp -> the cells' output channels.
+template <int EPI, int N>
+__device__ __forceinline__ void umma_epilogue(uint32_t taddr, const float* __restrict__ bias, void* __restrict__ out,
+                                              size_t pix, bool in_image, int cout_real, int out_stride)
+{
+    uint32_t r[N];
+    if constexpr (N == 32) {
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+            "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+              "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+              "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]),
+              "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]),
+              "=r"(r[30]), "=r"(r[31])
+            : "r"(taddr));
+    } else {
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+              "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+            : "r"(taddr));
+    }
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+    if (!in_image) return;
+    if constexpr (EPI == EPI_LINEAR_F32) {
+        float* o = reinterpret_cast<float*>(out) + pix * out_stride;
+#pragma unroll
+        for (int co = 0; co < N; co++)
+            if (co < cout_real) o[co] = __uint_as_float(r[co]) + __ldg(bias + co);
+    } else {
+        uint32_t packed[N / 2];
+#pragma unroll
+        for (int co = 0; co < N; co += 2)
+            packed[co / 2] = pack_bf16(fmaxf(__uint_as_float(r[co]) + __ldg(bias + co), 0.0f),
+                                       fmaxf(__uint_as_float(r[co + 1]) + __ldg(bias + co + 1), 0.0f));
+        uint4* o4 = reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(out) + pix * out_stride);
+#pragma unroll
+        for (int q = 0; q < N / 8; q++)
+            o4[q] = make_uint4(packed[4 * q], packed[4 * q + 1], packed[4 * q + 2], packed[4 * q + 3]);
+    }
+}
+
+__global__ void __launch_bounds__(128) k_net_fused(const __grid_constant__ NetFusedArgs a)
+{
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+    unsigned char* sA = sm;
+    unsigned char* sB = sm + 9 * U_TAP_A;
+    __shared__ __align__(8) uint64_t bar_load, bar_mma;
+    __shared__ uint32_t s_tmem;
+    __shared__ int s_ok;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int tiles_x = (a.w + UM - 1) / UM;
+    const int tiles = tiles_x * a.rows;
+
+    if (threadIdx.x == 0) {
+        mbar_init(&bar_load, 1);
+        mbar_init(&bar_mma, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        s_ok = 1;
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 32;" ::"r"(s_addr(&s_tmem))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = s_tmem;
+    uint32_t phase = 0;  // uses of bar_load / bar_mma so far (both advance together)
+
+    for (int l = 0; l < NL; l++) {
+        const int n = l == NL - 1 ? 16 : 32;
+        const int dil = a.dil[l];
+        bool weights_in = false;
+        for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+            const int row = tile / tiles_x;
+            const int x0 = (tile - row * tiles_x) * UM;
+            const int y = row % a.h;
+            if (threadIdx.x == 0 && s_ok) {
+                uint32_t taps = 0, bytes = weights_in ? 0u : 9u * n * 64;
+                for (int t = 0; t < 9; t++) {
+                    const int r = y + (t / 3 - 1) * dil;
+                    if (r >= 0 && r < a.h) {
+                        taps |= 1u << t;
+                        bytes += U_TAP_A;
+                    }
+                }
+                // reads of the previous layer's outputs go through the async proxy
+                asm volatile("fence.proxy.async.global;" ::: "memory");
+                mbar_expect_tx(&bar_load, bytes);
+                if (!weights_in) tma_load_3d(sB, &a.w_map[l], 0, 0, 0, &bar_load);
+                for (int t = 0; t < 9; t++)
+                    if (taps >> t & 1u)
+                        tma_load_3d(sA + t * U_TAP_A, &a.in_map[l], 0, x0 + (t % 3 - 1) * dil, row + (t / 3 - 1) * dil,
+                                    &bar_load);
+                if (mbar_wait(&bar_load, phase & 1u, a.polls)) {
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const uint32_t idesc = n == 16 ? umma_idesc(UM, 16) : umma_idesc(UM, 32);
+                    uint32_t acc = 0;
+                    for (int t = 0; t < 9; t++) {
+                        if (!(taps >> t & 1u)) continue;
+                        const uint32_t a0 = s_addr(sA + t * U_TAP_A), b0 = s_addr(sB + t * n * 64);
+#pragma unroll
+                        for (int kh = 0; kh < 2; kh++) {
+                            const uint64_t ad = umma_desc(a0 + kh * 32), bd = umma_desc(b0 + kh * 32);
+                            asm volatile(
+                                "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                                " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+                                ::"r"(tmem), "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+                                : "memory");
+                            acc = 1;
+                        }
+                    }
+                    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                                 ::"r"(s_addr(&bar_mma)) : "memory");
+                } else {
+                    atomicExch(a.err, 1);
+                    s_ok = 0;
+                    mbar_wait(&bar_load, phase & 1u, a.polls);
+                    mbar_arrive(&bar_mma);
+                }
+            }
+            weights_in = true;
+            __syncthreads();   // s_ok as thread 0 left it for this tile
+            if (!s_ok) break;
+            // tcgen05.ld is warp-collective: the block agrees on one outcome of the wait
+            const bool mine = mbar_wait(&bar_mma, phase & 1u, a.polls);
+            if (!__syncthreads_and(mine ? 1 : 0)) {
+                if (threadIdx.x == 0) {
+                    atomicExch(a.err, 2);
+                    s_ok = 0;
+                }
+                __syncthreads();
+            }
+            phase++;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const int x = x0 + warp * 32 + lane;
+            const size_t pix = (size_t)row * a.w + x;
+            const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+            if (s_ok) {
+                if (l == NL - 1)
+                    umma_epilogue<EPI_LINEAR_F32, 16>(taddr, a.bias[l], a.head, pix, x < a.w, 3, 3);
+                else
+                    umma_epilogue<EPI_RELU_BF16, 32>(taddr, a.bias[l], a.act[l], pix, x < a.w, 32, 32);
+            }
+            // the accumulator is read before the next tile's MMAs overwrite it
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncthreads();
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            if (!s_ok) break;
+        }
+        if (!s_ok) atomicExch(&a.bar->error, 1u);  // the others stop at the barrier
+        if (l == NL - 1) break;
+        // this layer's plain stores, before other CTAs read them through TMA
+        asm volatile("fence.proxy.async.global;" ::: "memory");
+        if (!net_grid_sync(a.bar, gridDim.x, a.polls)) {
+            if (threadIdx.x == 0) atomicExch(a.err, 3);
+            break;
+        }
+        if (!s_ok) break;
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 32;" ::"r"(tmem) : "memory");
+}
+
 // Dynamic shared-memory opt-in of every instantiation above 48 KB (once per process
 // and device; called from bm_net_create, outside any stream capture).
 cudaError_t conv_smem_optin()
@@ -740,9 +981,20 @@ cudaError_t conv_smem_optin()
         set((const void*)k_conv_umma<EPI_RELU_BF16, 32>, umma_smem(32)),
         set((const void*)k_conv_umma<EPI_MASK_BF16, 32>, umma_smem(32)),
         set((const void*)k_conv_umma<EPI_LINEAR_F32, 16>, umma_smem(16)),
+        set((const void*)k_net_fused, umma_smem(32)),
     };
     for (cudaError_t x : es)
         if (x != cudaSuccess) return x;
+    // the tcgen05 kernels take 93 KB each: ask for the largest shared-memory carve-out
+    // so that two CTAs share an SM (the fused launch then holds a 1024x436 frame's 218
+    // tiles in one wave)
+    const void* big[] = {(const void*)k_conv_umma<EPI_RELU_BF16, 32>, (const void*)k_conv_umma<EPI_MASK_BF16, 32>,
+                         (const void*)k_conv_umma<EPI_LINEAR_F32, 16>, (const void*)k_net_fused};
+    for (const void* f : big) {
+        const cudaError_t e2 = cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                                    (int)cudaSharedmemCarveoutMaxShared);
+        if (e2 != cudaSuccess) return e2;
+    }
     if (dev < 64) done[dev] = true;
     return cudaSuccess;
 }
@@ -773,6 +1025,9 @@ struct bm_net {
     // tcgen05 path (k_conv_umma): tensor maps of the weights (fixed buffers) and of the
     // activations for the last (B, h, w) seen; error word of its bounded waits
     bool umma = false;
+    bool fused = false;          // the six layers in one cooperative launch (k_net_fused)
+    int fused_grid_max = 0;      // co-resident CTAs of k_net_fused on this device
+    NetGridBar* d_bar = nullptr;
     int* d_err = nullptr;
     CUtensorMap map_wf[NL];
     CUtensorMap map_wb[NL];
@@ -844,6 +1099,39 @@ bm_status forward(bm_net* n, uint32_t B, uint32_t h, uint32_t w, cudaStream_t st
     const int Bi = (int)B, hi = (int)h, wi = (int)w;
     if (n->umma) {
         if (!ensure_act_maps(n, B, h, w)) return nfail(BM_ERR_CUDA, "bm_net: tensor map encoding failed");
+        if (n->fused) {
+            NetFusedArgs a;
+            for (int l = 0; l < NL; l++) {
+                a.in_map[l] = l == 0 ? n->map_in : n->map_act[l - 1];
+                a.w_map[l] = n->map_wf[l];
+                a.bias[l] = n->d_master + n->poff[l] + layer_w_count(l);
+                a.dil[l] = DIL[l];
+            }
+            for (int l = 0; l < NL - 1; l++) a.act[l] = n->d_act[l];
+            a.head = n->d_out;
+            a.h = hi;
+            a.w = wi;
+            a.rows = Bi * hi;
+            a.polls = U_POLLS;
+            a.bar = n->d_bar;
+            a.err = n->d_err;
+            const int tiles = ((wi + UM - 1) / UM) * Bi * hi;
+            const unsigned grid = (unsigned)std::min(tiles, n->fused_grid_max);
+            BN_CUDA(cudaMemsetAsync(n->d_bar, 0, sizeof(NetGridBar), st));
+            void* args[] = {(void*)&a};
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(grid);
+            cfg.blockDim = dim3(128);
+            cfg.dynamicSmemBytes = umma_smem(32);
+            cfg.stream = st;
+            cudaLaunchAttribute attr;
+            attr.id = cudaLaunchAttributeCooperative;
+            attr.val.cooperative = 1;
+            cfg.attrs = &attr;
+            cfg.numAttrs = 1;
+            BN_CUDA(cudaLaunchKernelExC(&cfg, (const void*)k_net_fused, args));
+            return BM_OK;
+        }
         for (int l = 0; l <= 4; l++)
             BN_CUDA((launch_conv_umma<EPI_RELU_BF16, 32>(l == 0 ? n->map_in : n->map_act[l - 1], n->map_wf[l],
                                                           n->d_master + n->poff[l] + layer_w_count(l), nullptr,
@@ -902,6 +1190,7 @@ bm_status bm_net_create(uint32_t max_batch, uint32_t max_h4, uint32_t max_w4, bm
              bmk::device_malloc((void**)&n->d_wb[l], (size_t)9 * CIN_P[l] * coutp16 * 2) == cudaSuccess;
     }
     if (ok) ok = bmk::device_malloc((void**)&n->d_err, sizeof(int)) == cudaSuccess;
+    if (ok) ok = bmk::device_malloc((void**)&n->d_bar, sizeof(NetGridBar)) == cudaSuccess;
     if (!ok) {
         bm_net_destroy(n);
         return nfail(BM_ERR_NOMEM, "bm_net_create: device allocation failed");
@@ -911,6 +1200,15 @@ bm_status bm_net_create(uint32_t max_batch, uint32_t max_h4, uint32_t max_w4, bm
     n->umma = true;
     for (int l = 0; n->umma && l < NL; l++) n->umma = weight_map(&n->map_wf[l], n->d_wf[l], COUT_P[l]);
     for (int l = 1; n->umma && l < NL - 1; l++) n->umma = weight_map(&n->map_wb[l], n->d_wb[l], CIN_P[l]);
+    {
+        int dev = 0, sms = 0, occ = 0, coop = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_net_fused, 128, umma_smem(32)) == cudaSuccess)
+            n->fused_grid_max = occ * sms;
+        n->fused = n->umma && coop && n->fused_grid_max > 0;
+    }
     cudaMemset(n->d_m, 0, off * 4);
     cudaMemset(n->d_v, 0, off * 4);
     cudaMemset(n->d_dy[0], 0, px * 32 * 2);
@@ -941,7 +1239,7 @@ bm_status bm_net_destroy(bm_net* n)
 {
     if (!n) return BM_OK;
     void* ptrs[] = {n->d_master, n->d_grad, n->d_m, n->d_v, n->d_in, n->d_out, n->d_loss, n->d_dy[0], n->d_dy[1],
-                    n->d_err};
+                    n->d_err, n->d_bar};
     for (void* q : ptrs)
         if (q) bmk::device_free(q);
     for (int l = 0; l < NL; l++) {
@@ -997,23 +1295,30 @@ bm_status bm_net_set_input(bm_net* n, const uint16_t* d_in, uint32_t B, uint32_t
     return BM_OK;
 }
 
-bm_status bm_net_set_umma(bm_net* n, int on)
+bm_status bm_net_set_umma(bm_net* n, int mode)
 {
     if (!n) return nfail(BM_ERR_INVALID, "bm_net_set_umma: null");
-    if (!on) {
+    if (mode < 0 || mode > 2) return nfail(BM_ERR_INVALID, "bm_net_set_umma: mode is 0, 1 or 2");
+    if (mode == 0) {
         n->umma = false;
+        n->fused = false;
         return BM_OK;
     }
+    if (mode == 2 && n->fused_grid_max <= 0)
+        return nfail(BM_ERR_CUDA, "bm_net_set_umma: no cooperative launch of the fused network on this device");
     bool ok = true;
     for (int l = 0; ok && l < NL; l++) ok = weight_map(&n->map_wf[l], n->d_wf[l], COUT_P[l]);
     for (int l = 1; ok && l < NL - 1; l++) ok = weight_map(&n->map_wb[l], n->d_wb[l], CIN_P[l]);
     if (!ok) return nfail(BM_ERR_CUDA, "bm_net_set_umma: tensor map encoding unavailable");
     n->umma = true;
+    n->fused = mode == 2;
     n->map_B = n->map_h = n->map_w = 0;
     return BM_OK;
 }
 
-int bm_net_umma(const bm_net* n) { return n && n->umma ? 1 : 0; }
+int bm_net_umma(const bm_net* n) { return !n || !n->umma ? 0 : n->fused ? 2 : 1; }
+
+int bm_net_fused_ctas(const bm_net* n) { return n ? n->fused_grid_max : 0; }
 
 bm_status bm_net_check(bm_net* n, void* stream)
 {
@@ -1024,8 +1329,9 @@ bm_status bm_net_check(bm_net* n, void* stream)
     if (h) {
         BN_CUDA(cudaMemsetAsync(n->d_err, 0, sizeof(int), (cudaStream_t)stream));
         BN_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
-        return nfail(BM_ERR_TIMEOUT, h == 1 ? "bm_net: a tensor-core layer's copies did not arrive in time"
-                                            : "bm_net: a tensor-core layer's MMA did not complete in time");
+        return nfail(BM_ERR_TIMEOUT, h == 1   ? "bm_net: a tensor-core layer's copies did not arrive in time"
+                                     : h == 2 ? "bm_net: a tensor-core layer's MMA did not complete in time"
+                                              : "bm_net: the fused network's grid barrier gave up");
     }
     return BM_OK;
 }

@@ -35,6 +35,7 @@ def _declare():
         "bm_net_set_umma": (c.c_int, [c.c_void_p, c.c_int]),
         "bm_net_umma": (c.c_int, [c.c_void_p]),
         "bm_net_check": (c.c_int, [c.c_void_p, c.c_void_p]),
+        "bm_net_fused_ctas": (c.c_int, [c.c_void_p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -104,13 +105,21 @@ class ProposalNet:
     def forward(self, B, h, w, d_out=0, stream=0):
         check(lib().bm_net_forward(self._n, B, h, w, ctypes.c_void_p(d_out), ctypes.c_void_p(stream)))
 
-    def set_umma(self, on=True):
-        """tcgen05 (on) or mma.sync (off) convolutions; see bm_net_set_umma."""
-        check(lib().bm_net_set_umma(self._n, int(bool(on))))
+    def set_umma(self, mode=2):
+        """Convolution path (bm_net_set_umma): 2 (or True) the fused cooperative tcgen05
+        forward, 1 tcgen05 per layer, 0 (or False) mma.sync."""
+        mode = 2 if mode is True else 0 if mode is False else int(mode)
+        check(lib().bm_net_set_umma(self._n, mode))
 
     @property
     def umma(self):
-        return bool(lib().bm_net_umma(self._n))
+        """The convolution path in use: 2, 1 or 0 (see set_umma)."""
+        return int(lib().bm_net_umma(self._n))
+
+    @property
+    def fused_ctas(self):
+        """Co-resident CTAs of the fused forward launch on this device."""
+        return int(lib().bm_net_fused_ctas(self._n))
 
     def check(self, stream=0):
         """Raises if a tensor-core layer's bounded wait gave up (bm_net_check)."""

@@ -82,13 +82,13 @@ def test_input_preparation():
     assert np.array_equal(o[..., 0], want_u) and np.array_equal(o[..., 1], want_v)
 
 
-def test_tcgen05_path_is_the_default():
+def test_fused_tcgen05_path_is_the_default():
     net = ProposalNet(1, 8, 8)
-    assert net.umma
+    assert net.umma == 2
     net.close()
 
 
-@pytest.mark.parametrize("umma", [True, False])
+@pytest.mark.parametrize("umma", [2, 1, 0])
 def test_forward_matches_oracle(umma):
     B, h, w = 2, 20, 36
     net, p, x, _ = _setup(B, h, w)
@@ -103,7 +103,7 @@ def test_forward_matches_oracle(umma):
     assert err < 2e-2, err
 
 
-@pytest.mark.parametrize("umma", [True, False])
+@pytest.mark.parametrize("umma", [2, 1, 0])
 def test_gradients_match_oracle(umma):
     B, h, w = 2, 20, 36
     net, p, x, tgt = _setup(B, h, w, seed=1)
@@ -136,15 +136,18 @@ def test_training_reduces_loss():
     assert last[0] < 0.8 * first[0]
 
 
-@pytest.mark.parametrize("B,h,w", [(1, 109, 256), (2, 7, 300), (3, 5, 17)])
-def test_tcgen05_equals_mma_sync(B, h, w):
-    """Whole 128-cell tiles, a ragged last tile and an image narrower than one tile:
-    the tcgen05 forward and training step equal the mma.sync ones up to FP32 summation
-    order (both round activations to BF16 between layers)."""
+@pytest.mark.parametrize("B,h,w", [(1, 109, 256), (2, 7, 300), (3, 5, 17), (1, 300, 480)])
+@pytest.mark.parametrize("mode", [2, 1])
+def test_tcgen05_equals_mma_sync(mode, B, h, w):
+    """Whole 128-cell tiles, a ragged last tile, an image narrower than one tile and
+    one with more tiles than co-resident CTAs (each CTA of the fused launch then walks
+    several tiles per layer): the tcgen05 forward and training step equal the
+    mma.sync ones up to FP32 summation order (both round activations to BF16 between
+    layers)."""
     net, p, x, tgt = _setup(B, h, w, seed=3)
     d_t = torch.from_numpy(tgt).cuda()
     outs, grads = [], []
-    for umma in (True, False):
+    for umma in (mode, 0):
         net.set_umma(umma)
         out = torch.empty(B, h, w, 3, device="cuda")
         net.forward(B, h, w, out.data_ptr())
