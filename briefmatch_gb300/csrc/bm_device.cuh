@@ -684,52 +684,64 @@ __device__ __forceinline__ void trilateral_block(const float* __restrict__ U, co
     const f2x kEE = pk2(kE, kE), kII = pk2(kI, kI), rr = pk2(r_, r_);
     f2x ufA = 0, ufB = 0, vfA = 0, vfB = 0, WA = 0, WB = 0;  // 0 bits = (0.0f, 0.0f)
     const int row0 = threadIdx.y * TRI_R;
-    for (int i = -s; i < s; i++) {
+    // two source columns (i, i + 1) per step (2s is even): twice the independent
+    // accumulation chains per thread, to keep the FMA pipe fed between the exp2s
+    for (int i = -s; i < s; i += 2) {
         const float2* col = suv + row0 * TW + threadIdx.x + s + i;
         const float* colI = sI + row0 * TW + threadIdx.x + s + i;
-        f2x cuA = 0, cuB = 0, cvA = 0, cvB = 0, cwA = 0, cwB = 0;
+        f2x cuA[2] = {0, 0}, cuB[2] = {0, 0}, cvA[2] = {0, 0}, cvB[2] = {0, 0}, cwA[2] = {0, 0}, cwB[2] = {0, 0};
         // source row m lies in output r's window when 0 <= m - r < 2s: pair A (outputs
         // 0, 1) has none of its rows past m = 2s, pair B (outputs 2, 3) none before
         // m = 2; those evaluations would add exact zeros and are skipped
-        auto tap = [&](int m, auto doA, auto doB) {
-            const float2 uv = col[m * TW];
-            const float i1 = colI[m * TW];
+        auto tap = [&](int m, int c, auto doA, auto doB) {
+            const float2 uv = col[m * TW + c];
+            const float i1 = colI[m * TW + c];
             const float4 rf = rowf[m];
             const f2x uu = pk2(uv.x, uv.x), vv = pk2(uv.y, uv.y), ii = pk2(i1, i1);
             if constexpr (decltype(doA)::value) {
                 const f2x du = fma2(uu, kEE, umA), dv = fma2(vv, kEE, vmA), dI = fma2(ii, kII, IA);
                 const f2x q = fma2(dI, dI, fma2(dv, dv, fma2(du, du, pk2(rf.x, rf.y))));
                 const f2x w = ex2n_2(mul2(q, rr));
-                cuA = fma2(w, uu, cuA);
-                cvA = fma2(w, vv, cvA);
-                cwA = add2(cwA, w);
+                cuA[c] = fma2(w, uu, cuA[c]);
+                cvA[c] = fma2(w, vv, cvA[c]);
+                cwA[c] = add2(cwA[c], w);
             }
             if constexpr (decltype(doB)::value) {
                 const f2x du = fma2(uu, kEE, umB), dv = fma2(vv, kEE, vmB), dI = fma2(ii, kII, IB);
                 const f2x q = fma2(dI, dI, fma2(dv, dv, fma2(du, du, pk2(rf.z, rf.w))));
                 const f2x w = ex2n_2(mul2(q, rr));
-                cuB = fma2(w, uu, cuB);
-                cvB = fma2(w, vv, cvB);
-                cwB = add2(cwB, w);
+                cuB[c] = fma2(w, uu, cuB[c]);
+                cvB[c] = fma2(w, vv, cvB[c]);
+                cwB[c] = add2(cwB[c], w);
             }
         };
         static_assert(TRI_R == 4, "the row split below assumes two output pairs");
         using yes = std::true_type;
         using no = std::false_type;
-        tap(0, yes{}, no{});
-        tap(1, yes{}, no{});
-#pragma unroll 4
-        for (int m = 2; m <= 2 * s; m++) tap(m, yes{}, yes{});
-        tap(2 * s + 1, no{}, yes{});
-        tap(2 * s + 2, no{}, yes{});
-        const float wi = exp2f(-(float)(i * i) * cS);
-        const f2x wi2 = pk2(wi, wi);
-        ufA = fma2(wi2, cuA, ufA);
-        ufB = fma2(wi2, cuB, ufB);
-        vfA = fma2(wi2, cvA, vfA);
-        vfB = fma2(wi2, cvB, vfB);
-        WA = fma2(wi2, cwA, WA);
-        WB = fma2(wi2, cwB, WB);
+        tap(0, 0, yes{}, no{});
+        tap(0, 1, yes{}, no{});
+        tap(1, 0, yes{}, no{});
+        tap(1, 1, yes{}, no{});
+#pragma unroll 2
+        for (int m = 2; m <= 2 * s; m++) {
+            tap(m, 0, yes{}, yes{});
+            tap(m, 1, yes{}, yes{});
+        }
+        tap(2 * s + 1, 0, no{}, yes{});
+        tap(2 * s + 1, 1, no{}, yes{});
+        tap(2 * s + 2, 0, no{}, yes{});
+        tap(2 * s + 2, 1, no{}, yes{});
+#pragma unroll
+        for (int c = 0; c < 2; c++) {
+            const float wi = exp2f(-(float)((i + c) * (i + c)) * cS);
+            const f2x wi2 = pk2(wi, wi);
+            ufA = fma2(wi2, cuA[c], ufA);
+            ufB = fma2(wi2, cuB[c], ufB);
+            vfA = fma2(wi2, cvA[c], vfA);
+            vfB = fma2(wi2, cvB[c], vfB);
+            WA = fma2(wi2, cwA[c], WA);
+            WB = fma2(wi2, cwB[c], WB);
+        }
     }
     const float uf[TRI_R] = {lo2(ufA), hi2(ufA), lo2(ufB), hi2(ufB)};
     const float vf[TRI_R] = {lo2(vfA), hi2(vfA), lo2(vfB), hi2(vfB)};

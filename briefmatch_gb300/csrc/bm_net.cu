@@ -1027,7 +1027,6 @@ struct bm_net {
     bool umma = false;
     bool fused = false;          // the six layers in one cooperative launch (k_net_fused)
     int fused_grid_max = 0;      // co-resident CTAs of k_net_fused on this device
-    int fused_grid_try = 0;      // the larger grid the shared memory per SM allows, tried first
     NetGridBar* d_bar = nullptr;
     int* d_err = nullptr;
     CUtensorMap map_wf[NL];
@@ -1128,15 +1127,8 @@ bm_status forward(bm_net* n, uint32_t B, uint32_t h, uint32_t w, cudaStream_t st
             attr.val.cooperative = 1;
             cfg.attrs = &attr;
             cfg.numAttrs = 1;
-            cfg.gridDim = dim3((unsigned)std::min(tiles, std::max(n->fused_grid_try, n->fused_grid_max)));
-            cudaError_t e = cudaLaunchKernelExC(&cfg, (const void*)k_net_fused, args);
-            if (e == cudaErrorCooperativeLaunchTooLarge && n->fused_grid_try > n->fused_grid_max) {
-                cudaGetLastError();  // a configuration error, nothing was launched
-                n->fused_grid_try = n->fused_grid_max;
-                cfg.gridDim = dim3((unsigned)std::min(tiles, n->fused_grid_max));
-                e = cudaLaunchKernelExC(&cfg, (const void*)k_net_fused, args);
-            }
-            BN_CUDA(e);
+            cfg.gridDim = dim3((unsigned)std::min(tiles, n->fused_grid_max));
+            BN_CUDA(cudaLaunchKernelExC(&cfg, (const void*)k_net_fused, args));
             return BM_OK;
         }
         for (int l = 0; l <= 4; l++)
@@ -1208,21 +1200,15 @@ bm_status bm_net_create(uint32_t max_batch, uint32_t max_h4, uint32_t max_w4, bm
     for (int l = 0; n->umma && l < NL; l++) n->umma = weight_map(&n->map_wf[l], n->d_wf[l], COUT_P[l]);
     for (int l = 1; n->umma && l < NL - 1; l++) n->umma = weight_map(&n->map_wb[l], n->d_wb[l], CIN_P[l]);
     {
-        // co-resident CTAs of the fused launch: the occupancy calculator's figure, and
-        // the one the shared memory per SM allows (the launch tries the latter first
-        // and keeps the former if the runtime rejects it)
-        int dev = 0, sms = 0, occ = 0, coop = 0, smem_sm = 0, reserved = 0;
+        // co-resident CTAs of the fused launch (mode 2); the per-layer launches (mode 1)
+        // measured faster and are the default
+        int dev = 0, sms = 0, occ = 0, coop = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
-        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
-        cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_net_fused, 128, umma_smem(32)) != cudaSuccess) occ = 0;
-        const size_t per_cta = umma_smem(32) + 64 + (size_t)reserved;
-        const int by_smem = std::min(4, (int)((size_t)smem_sm / per_cta));
-        n->fused_grid_max = occ * sms;
-        n->fused_grid_try = std::max(occ, by_smem) * sms;
-        n->fused = n->umma && coop && n->fused_grid_max > 0;
+        if (coop && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_net_fused, 128, umma_smem(32)) == cudaSuccess)
+            n->fused_grid_max = occ * sms;
+        n->fused = false;
     }
     cudaMemset(n->d_m, 0, off * 4);
     cudaMemset(n->d_v, 0, off * 4);
@@ -1333,7 +1319,7 @@ bm_status bm_net_set_umma(bm_net* n, int mode)
 
 int bm_net_umma(const bm_net* n) { return !n || !n->umma ? 0 : n->fused ? 2 : 1; }
 
-int bm_net_fused_ctas(const bm_net* n) { return n ? std::max(n->fused_grid_try, n->fused_grid_max) : 0; }
+int bm_net_fused_ctas(const bm_net* n) { return n ? n->fused_grid_max : 0; }
 
 bm_status bm_net_check(bm_net* n, void* stream)
 {

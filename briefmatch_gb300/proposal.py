@@ -105,10 +105,10 @@ class ProposalNet:
     def forward(self, B, h, w, d_out=0, stream=0):
         check(lib().bm_net_forward(self._n, B, h, w, ctypes.c_void_p(d_out), ctypes.c_void_p(stream)))
 
-    def set_umma(self, mode=2):
-        """Convolution path (bm_net_set_umma): 2 (or True) the fused cooperative tcgen05
-        forward, 1 tcgen05 per layer, 0 (or False) mma.sync."""
-        mode = 2 if mode is True else 0 if mode is False else int(mode)
+    def set_umma(self, mode=1):
+        """Convolution path (bm_net_set_umma): 1 (or True; the default) tcgen05 per layer,
+        2 the fused cooperative tcgen05 forward, 0 (or False) mma.sync."""
+        mode = 1 if mode is True else 0 if mode is False else int(mode)
         check(lib().bm_net_set_umma(self._n, mode))
 
     @property

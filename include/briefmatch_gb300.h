@@ -330,17 +330,18 @@ bm_status bm_net_forward(bm_net* n, uint32_t B, uint32_t h, uint32_t w, float* d
  * h_loss (may be NULL) receives (flow loss, confidence loss, confident fraction). */
 bm_status bm_net_train_step(bm_net* n, uint32_t B, uint32_t h, uint32_t w, const float* d_target, float lr,
                             float* d_grad_out, float* h_loss, void* stream);
-/* Which tensor-core path the convolutions take.  mode 2 (the default where the driver
- * encodes tensor maps and the device launches cooperative kernels): the forward pass
- * is one cooperative launch of tcgen05 MMAs into tensor memory fed by TMA, all six
- * layers with a grid barrier between them; mode 1: the same MMAs, one launch per
- * layer; mode 0: mma.sync m16n8k16 kernels.  The backward-data pass of the 32-channel
- * layers runs on tcgen05 in modes 1 and 2.  All modes give the same network up to
- * FP32 summation order.  bm_net_umma returns the mode in use. */
+/* Which tensor-core path the convolutions take.  mode 1 (the default where the driver
+ * encodes tensor maps): every layer of the forward pass, and the backward-data pass of
+ * the 32-channel layers, is a launch of tcgen05 MMAs into tensor memory fed by TMA;
+ * mode 2: the six forward layers in one cooperative launch of the same MMAs with a
+ * grid barrier between layers (measured slower than mode 1 at 1024x436: the barrier
+ * costs more than the launches it saves); mode 0: mma.sync m16n8k16 kernels.  All
+ * modes give the same network up to FP32 summation order.  bm_net_umma returns the
+ * mode in use. */
 bm_status bm_net_set_umma(bm_net* n, int mode);
 int bm_net_umma(const bm_net* n);
-/* CTAs the mode-2 launch can keep co-resident on this device (it walks the layer's
- * 128-cell tiles with that grid). */
+/* CTAs the mode-2 launch keeps co-resident on this device (it walks each layer's
+ * 128-cell tiles with that grid); 0 where cooperative launches are unavailable. */
 int bm_net_fused_ctas(const bm_net* n);
 /* Synchronises `stream` and reports BM_ERR_TIMEOUT if a tensor-core layer's bounded
  * wait for its copies, its MMAs or (mode 2) the grid barrier gave up since the last

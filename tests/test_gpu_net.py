@@ -82,9 +82,10 @@ def test_input_preparation():
     assert np.array_equal(o[..., 0], want_u) and np.array_equal(o[..., 1], want_v)
 
 
-def test_fused_tcgen05_path_is_the_default():
+def test_tcgen05_path_is_the_default():
     net = ProposalNet(1, 8, 8)
-    assert net.umma == 2
+    assert net.umma == 1
+    assert net.fused_ctas >= 152  # the fused launch is available as mode 2
     net.close()
 
 
