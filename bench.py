@@ -527,11 +527,14 @@ def run_engine(args, torch, world, rank):
             sch, table = choose_schedule(torch, prm, pattern, net, stream)
         # the network's forward on both tensor-core paths (tcgen05 is the engine's)
         nf = {}
-        for path, mode in (("mma_sync", 0), ("tcgen05_per_layer", 1), ("tcgen05_fused", 2)):
+        default_mode = net.umma
+        for path, mode in (("mma_sync", 0), ("tcgen05_fused", 2), ("tcgen05_per_layer", 1)):
             net.set_umma(mode)
             nf[path] = net_forward_timing(torch, net, d_frames, stream)
+        net.set_umma(default_mode)  # the engines below run the network's default path
         net.check(stream.cuda_stream)
         nf["tcgen05_fused"]["ctas"] = net.fused_ctas
+        nf["engine_path"] = {2: "tcgen05_fused", 1: "tcgen05_per_layer", 0: "mma_sync"}[net.umma]
         learned = {"weights": os.path.relpath(learn.DEFAULT_WEIGHTS, ROOT), "confidence": PROPOSAL_CONF,
                    "calibration": table, "schedule": None, "net_forward": nf}
         if sch is not None:

@@ -119,6 +119,12 @@ struct bm_ctx {
     uint32_t net_iterations = 0, net_jfMax = 0;
     uint32_t local_steps = 0, local_radius = 1;   // bm_set_local_steps
     float* d_pred = nullptr;   // [h4][w4][3]
+    // the network runs on a side stream, concurrently with the frame's up-sampling and
+    // descriptors: it starts once both 8-bit frames are on the device (ev_u8) and the
+    // seed waits for it (ev_net)
+    cudaStream_t net_stream = nullptr;
+    cudaEvent_t ev_u8 = nullptr, ev_net = nullptr;
+    bool net_pending = false;   // ev_net recorded for this frame, not yet waited on
 
     // colour coding (bm_colors), allocated on first use
     int* d_color_word = nullptr;    // largest vector length, float bits
@@ -223,10 +229,11 @@ void release(bm_ctx* c)
     }
     for (cudaEvent_t e : c->prof_pool) cudaEventDestroy(e);
     cudaEvent_t evs[] = {c->ev_ready, c->ev_refined, c->ev_frame_free[0], c->ev_frame_free[1], c->ev_frame_free[2],
-                         c->ev_flowin_free[0], c->ev_flowin_free[1]};
+                         c->ev_flowin_free[0], c->ev_flowin_free[1], c->ev_u8, c->ev_net};
     for (cudaEvent_t e : evs)
         if (e) cudaEventDestroy(e);
     if (c->refine_stream) cudaStreamDestroy(c->refine_stream);
+    if (c->net_stream) cudaStreamDestroy(c->net_stream);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
 }
 
@@ -330,6 +337,10 @@ bm_status match_impl(bm_ctx* c, const float* d_im2, bool seeded, bool padded = f
     if (seeded) {
         const int w4 = (int)p.sx_in / 4, h4 = (int)p.sy_in / 4;
         const float scx = 4.0f * (float)p.sx / (float)p.sx_in, scy = 4.0f * (float)p.sy / (float)p.sy_in;
+        if (c->net_pending) {  // the proposal computed on the side stream
+            BM_CUDA(cudaStreamWaitEvent(c->stream, c->ev_net, 0));
+            c->net_pending = false;
+        }
         BM_LAUNCH(c, "seed", bmk::seed_field(c->feat1_ptr(), c->feat2_ptr(), c->d_flow[c->flow_cur], c->d_flow[c->flow_cur ^ 1],
                                              c->d_cost, (int)p.sx, (int)p.sy, (int)c->nsp, first, c->d_pred, w4, h4, scx,
                                              scy, c->net_logit_min, c->stream));
@@ -895,6 +906,12 @@ bm_status bm_set_proposal(bm_ctx* c, bm_net* net, float conf_threshold, uint32_t
     if (net && !(conf_threshold > 0.0f && conf_threshold < 1.0f))
         return fail(BM_ERR_INVALID, "bm_set_proposal: confidence threshold must lie in (0, 1)");
     if (net && (c->prm.sx_in < 4 || c->prm.sy_in < 4)) return fail(BM_ERR_LIMIT, "bm_set_proposal: frame too small");
+    if (net && !c->net_stream) {
+        cudaError_t e = cudaStreamCreateWithFlags(&c->net_stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_u8, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_net, cudaEventDisableTiming);
+        if (e != cudaSuccess) return fail(BM_ERR_CUDA, "bm_set_proposal: %s", cudaGetErrorString(e));
+    }
     c->net = net;
     c->net_logit_min = net ? std::log(conf_threshold / (1.0f - conf_threshold)) : 0.0f;
     c->net_iterations = iterations;
@@ -994,6 +1011,20 @@ bm_status bm_frame(bm_ctx* c, const uint8_t* frame, int frame_on_device, float* 
     uint8_t* d_u8 = c->d_u8[slot];
     BM_CUDA(cudaMemcpyAsync(d_u8, frame, ni, frame_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
                             c->stream));
+    const bool seeded = c->primed && c->net != nullptr;
+    if (seeded) {
+        // the proposal network on its side stream, from the previous and this frame,
+        // while this stream up-samples and describes the frame; match_impl's seed waits
+        const uint32_t w4 = p.sx_in / 4, h4 = p.sy_in / 4;
+        BM_CUDA(cudaEventRecord(c->ev_u8, c->stream));
+        BM_CUDA(cudaStreamWaitEvent(c->net_stream, c->ev_u8, 0));
+        bm_status nst = bm_net_prepare(c->net, 0, c->d_u8[prev], d_u8, p.sx_in, p.sy_in, c->net_stream);
+        if (nst == BM_OK) nst = bm_net_forward(c->net, 1, h4, w4, c->d_pred, c->net_stream);
+        if (nst != BM_OK) return nst;
+        BM_CUDA(cudaEventRecord(c->ev_net, c->net_stream));
+        c->net_pending = true;
+        c->launches += 7;
+    }
     float* cur = c->d_frame[slot];
     BM_LAUNCH(c, "u8_to_f32", bmk::u8_to_f32(d_u8, cur, ni, c->stream));
     // of_pipeline.cpp:301-310
@@ -1015,14 +1046,6 @@ bm_status bm_frame(bm_ctx* c, const uint8_t* frame, int frame_on_device, float* 
         BM_CUDA(cudaMemsetAsync(c->d_flow_out, 0, 2 * ni * sizeof(float), c->stream));
         c->primed = true;
     } else {
-        const bool seeded = c->net != nullptr;
-        if (seeded) {
-            const uint32_t w4 = p.sx_in / 4, h4 = p.sy_in / 4;
-            st = bm_net_prepare(c->net, 0, c->d_u8[prev], d_u8, p.sx_in, p.sy_in, c->stream);
-            if (st == BM_OK) st = bm_net_forward(c->net, 1, h4, w4, c->d_pred, c->stream);
-            if (st != BM_OK) return st;
-            c->launches += 7;
-        }
         st = match_impl(c, up, seeded, padded);                   // of_pipeline.cpp:314
         if (st != BM_OK) return st;
         if (c->pipelined) {
