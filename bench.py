@@ -388,7 +388,14 @@ def measure(args, torch, world, eng, d_frames, flows, stream, flush):
         return total_ms / args.steps, launches, clk.summary(), kstats
 
     ms, launches, clocks, _ = timed(False)
+    # the per-kernel profile (roofline, kernel table) with each frame finished before
+    # the next: with pipelined frames a launch's events would also span the work of
+    # the other stream running beside it
+    if PIPELINED:
+        eng.set_pipelined(False)
     ms_prof, _, _, kstats = timed(True)
+    if PIPELINED:
+        eng.set_pipelined(True)
     u, v = d_u.cpu().numpy(), d_v.cpu().numpy()
     return {"ms_per_step": ms, "value": aggregate_value(world, npairs * W * H, ms), "launches": launches,
             "kstats": kstats, "ms_per_step_profiled": ms_prof, "clocks": clocks, "epe": mean_epe(u, v, flows),
@@ -558,9 +565,9 @@ def run_engine(args, torch, world, rank):
     ranked = sorted(kstats.items(), key=lambda kv: -kv[1][1])
     dom, (n_launch, dom_ms) = ranked[0]
     roofline = roofline_entry(torch, dom, n_launch, dom_ms, total_k, prm, head["clocks"])
-    roofline["timed_region"] = ("second run of the K timed steps with a CUDA event pair around every launch "
-                                "(%.3f ms per step there vs %.3f without); with pipelined frames the refinement "
-                                "overlaps matching, so launch times include the sharing"
+    roofline["timed_region"] = ("second run of the K timed steps with a CUDA event pair around every launch, frames "
+                                "not pipelined so that no other kernel shares a launch's time (%.3f ms per step "
+                                "there vs %.3f in the pipelined timed run)"
                                 % (head["ms_per_step_profiled"], head["ms_per_step"]))
     # the other large kernels' rooflines beside the dominant one
     roofline["others"] = [roofline_entry(torch, k, c, t, total_k, prm, head["clocks"]) for k, (c, t) in ranked[1:4]]

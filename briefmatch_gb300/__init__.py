@@ -107,6 +107,7 @@ def _declare(lib):
         "bm_profile_reset": (c.c_int, [c.c_void_p]),
         "bm_profile_read": (c.c_int, [c.c_void_p, c.c_void_p, c.c_uint32, P(c.c_uint32)]),
         "bm_set_proposal": (c.c_int, [c.c_void_p, c.c_void_p, c.c_float, c.c_uint32, c.c_uint32]),
+        "bm_set_proposal_stream": (c.c_int, [c.c_void_p, c.c_int]),
         "bm_set_pipelined": (c.c_int, [c.c_void_p, c.c_int]),
         "bm_set_local_steps": (c.c_int, [c.c_void_p, c.c_uint32, c.c_uint32]),
         "bm_local_step": (c.c_int, [c.c_void_p, c.c_uint32]),
@@ -532,6 +533,12 @@ class Batch:
         """Seed every pair with a ProposalNet (None detaches); see bm_batch_set_proposal."""
         check(lib().bm_batch_set_proposal(self._b, net.handle if net is not None else None, conf_threshold,
                                           iterations, jf_max))
+
+
+def set_proposal_stream(engine, side=True):
+    """Whether the context runs the proposal network on its own side stream
+    (bm_set_proposal_stream; the default) or on the context stream."""
+    check(lib().bm_set_proposal_stream(engine.ctx, int(bool(side))))
 
 
 def set_proposal(engine, net, conf_threshold=0.5, iterations=1, jf_max=16):

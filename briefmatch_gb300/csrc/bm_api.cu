@@ -125,6 +125,7 @@ struct bm_ctx {
     cudaStream_t net_stream = nullptr;
     cudaEvent_t ev_u8 = nullptr, ev_net = nullptr;
     bool net_pending = false;   // ev_net recorded for this frame, not yet waited on
+    bool net_side = true;       // bm_set_proposal_stream
 
     // colour coding (bm_colors), allocated on first use
     int* d_color_word = nullptr;    // largest vector length, float bits
@@ -919,6 +920,13 @@ bm_status bm_set_proposal(bm_ctx* c, bm_net* net, float conf_threshold, uint32_t
     return BM_OK;
 }
 
+bm_status bm_set_proposal_stream(bm_ctx* c, int side)
+{
+    if (check_ctx(c)) return BM_ERR_INVALID;
+    c->net_side = side != 0;
+    return BM_OK;
+}
+
 bm_status bm_set_local_steps(bm_ctx* c, uint32_t count, uint32_t first_radius)
 {
     if (check_ctx(c)) return BM_ERR_INVALID;
@@ -1012,7 +1020,7 @@ bm_status bm_frame(bm_ctx* c, const uint8_t* frame, int frame_on_device, float* 
     BM_CUDA(cudaMemcpyAsync(d_u8, frame, ni, frame_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
                             c->stream));
     const bool seeded = c->primed && c->net != nullptr;
-    if (seeded) {
+    if (seeded && c->net_side) {
         // the proposal network on its side stream, from the previous and this frame,
         // while this stream up-samples and describes the frame; match_impl's seed waits
         const uint32_t w4 = p.sx_in / 4, h4 = p.sy_in / 4;
@@ -1046,6 +1054,13 @@ bm_status bm_frame(bm_ctx* c, const uint8_t* frame, int frame_on_device, float* 
         BM_CUDA(cudaMemsetAsync(c->d_flow_out, 0, 2 * ni * sizeof(float), c->stream));
         c->primed = true;
     } else {
+        if (seeded && !c->net_side) {  // the network on the context stream, after up-sampling
+            const uint32_t w4 = p.sx_in / 4, h4 = p.sy_in / 4;
+            st = bm_net_prepare(c->net, 0, c->d_u8[prev], d_u8, p.sx_in, p.sy_in, c->stream);
+            if (st == BM_OK) st = bm_net_forward(c->net, 1, h4, w4, c->d_pred, c->stream);
+            if (st != BM_OK) return st;
+            c->launches += 7;
+        }
         st = match_impl(c, up, seeded, padded);                   // of_pipeline.cpp:314
         if (st != BM_OK) return st;
         if (c->pipelined) {

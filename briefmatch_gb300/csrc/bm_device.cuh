@@ -684,12 +684,16 @@ __device__ __forceinline__ void trilateral_block(const float* __restrict__ U, co
     const f2x kEE = pk2(kE, kE), kII = pk2(kI, kI), rr = pk2(r_, r_);
     f2x ufA = 0, ufB = 0, vfA = 0, vfB = 0, WA = 0, WB = 0;  // 0 bits = (0.0f, 0.0f)
     const int row0 = threadIdx.y * TRI_R;
-    // two source columns (i, i + 1) per step (2s is even): twice the independent
-    // accumulation chains per thread, to keep the FMA pipe fed between the exp2s
-    for (int i = -s; i < s; i += 2) {
+    // NC source columns (i .. i + NC - 1) per step: NC times the independent
+    // accumulation chains of a one-column walk, to keep the FMA pipe fed between the
+    // exp2s (three measured fastest; the last 2s mod 3 columns go one at a time)
+    auto columns = [&](int i, auto ncols) {
+        constexpr int NC = decltype(ncols)::value;
         const float2* col = suv + row0 * TW + threadIdx.x + s + i;
         const float* colI = sI + row0 * TW + threadIdx.x + s + i;
-        f2x cuA[2] = {0, 0}, cuB[2] = {0, 0}, cvA[2] = {0, 0}, cvB[2] = {0, 0}, cwA[2] = {0, 0}, cwB[2] = {0, 0};
+        f2x cuA[NC], cuB[NC], cvA[NC], cvB[NC], cwA[NC], cwB[NC];
+#pragma unroll
+        for (int c = 0; c < NC; c++) cuA[c] = cuB[c] = cvA[c] = cvB[c] = cwA[c] = cwB[c] = 0;
         // source row m lies in output r's window when 0 <= m - r < 2s: pair A (outputs
         // 0, 1) has none of its rows past m = 2s, pair B (outputs 2, 3) none before
         // m = 2; those evaluations would add exact zeros and are skipped
@@ -718,21 +722,23 @@ __device__ __forceinline__ void trilateral_block(const float* __restrict__ U, co
         static_assert(TRI_R == 4, "the row split below assumes two output pairs");
         using yes = std::true_type;
         using no = std::false_type;
-        tap(0, 0, yes{}, no{});
-        tap(0, 1, yes{}, no{});
-        tap(1, 0, yes{}, no{});
-        tap(1, 1, yes{}, no{});
+#pragma unroll
+        for (int c = 0; c < NC; c++) {
+            tap(0, c, yes{}, no{});
+            tap(1, c, yes{}, no{});
+        }
 #pragma unroll 2
         for (int m = 2; m <= 2 * s; m++) {
-            tap(m, 0, yes{}, yes{});
-            tap(m, 1, yes{}, yes{});
-        }
-        tap(2 * s + 1, 0, no{}, yes{});
-        tap(2 * s + 1, 1, no{}, yes{});
-        tap(2 * s + 2, 0, no{}, yes{});
-        tap(2 * s + 2, 1, no{}, yes{});
 #pragma unroll
-        for (int c = 0; c < 2; c++) {
+            for (int c = 0; c < NC; c++) tap(m, c, yes{}, yes{});
+        }
+#pragma unroll
+        for (int c = 0; c < NC; c++) {
+            tap(2 * s + 1, c, no{}, yes{});
+            tap(2 * s + 2, c, no{}, yes{});
+        }
+#pragma unroll
+        for (int c = 0; c < NC; c++) {
             const float wi = exp2f(-(float)((i + c) * (i + c)) * cS);
             const f2x wi2 = pk2(wi, wi);
             ufA = fma2(wi2, cuA[c], ufA);
@@ -742,7 +748,10 @@ __device__ __forceinline__ void trilateral_block(const float* __restrict__ U, co
             WA = fma2(wi2, cwA[c], WA);
             WB = fma2(wi2, cwB[c], WB);
         }
-    }
+    };
+    int i = -s;
+    for (; i + 3 <= s; i += 3) columns(i, std::integral_constant<int, 3>{});
+    for (; i < s; i++) columns(i, std::integral_constant<int, 1>{});
     const float uf[TRI_R] = {lo2(ufA), hi2(ufA), lo2(ufB), hi2(ufB)};
     const float vf[TRI_R] = {lo2(vfA), hi2(vfA), lo2(vfB), hi2(vfB)};
     const float W[TRI_R] = {lo2(WA), hi2(WA), lo2(WB), hi2(WB)};

@@ -27,12 +27,13 @@ def _frames(n=7):
     return frames, d
 
 
-def _run(d, pipelined, net=None, host=False, switch_off_at=None):
+def _run(d, pipelined, net=None, host=False, switch_off_at=None, side=True):
     prm = bm.BMParams.derive(W, H, 2.0, 2.0, N=64)
     eng = bm.BriefMatch(prm)
     eng.setup()
     if net is not None:
         bm.set_proposal(eng, net, 0.5, 1, 8)
+        bm.set_proposal_stream(eng, side)
     eng.set_pipelined(pipelined)
     n = len(d) - 1
     if host:
@@ -90,3 +91,16 @@ def test_pipelined_stage_reads_wait():
         u, v = ref.process_frame(f)
         assert np.array_equal(outs[k][0], u) and np.array_equal(outs[k][1], v), k
     ref.clean()
+
+
+@pytest.mark.parametrize("pipelined", [False, True])
+def test_proposal_side_stream_equals_context_stream(pipelined):
+    """The network on the context's side stream (concurrent with up-sampling and
+    descriptors) gives the same flows as on the context stream."""
+    _, d = _frames()
+    net = learn.load_net(learn.DEFAULT_WEIGHTS, 1, H // 4, W // 4)
+    ref = _run(d, pipelined, net=net, side=False)
+    got = _run(d, pipelined, net=net, side=True)
+    for a, b in zip(ref, got):
+        assert np.array_equal(a, b)
+    net.close()
