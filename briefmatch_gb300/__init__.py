@@ -536,8 +536,8 @@ class Batch:
 
 
 def set_proposal_stream(engine, side=True):
-    """Whether the context runs the proposal network on its own side stream
-    (bm_set_proposal_stream; the default) or on the context stream."""
+    """Whether the context runs the proposal network on its own side stream or on the
+    context stream (bm_set_proposal_stream; the context stream is the default)."""
     check(lib().bm_set_proposal_stream(engine.ctx, int(bool(side))))
 
 

@@ -119,13 +119,13 @@ struct bm_ctx {
     uint32_t net_iterations = 0, net_jfMax = 0;
     uint32_t local_steps = 0, local_radius = 1;   // bm_set_local_steps
     float* d_pred = nullptr;   // [h4][w4][3]
-    // the network runs on a side stream, concurrently with the frame's up-sampling and
-    // descriptors: it starts once both 8-bit frames are on the device (ev_u8) and the
-    // seed waits for it (ev_net)
+    // with bm_set_proposal_stream(ctx, 1) the network runs on a side stream,
+    // concurrently with the frame's up-sampling and descriptors: it starts once both
+    // 8-bit frames are on the device (ev_u8) and the seed waits for it (ev_net)
     cudaStream_t net_stream = nullptr;
     cudaEvent_t ev_u8 = nullptr, ev_net = nullptr;
     bool net_pending = false;   // ev_net recorded for this frame, not yet waited on
-    bool net_side = true;       // bm_set_proposal_stream
+    bool net_side = false;      // bm_set_proposal_stream (measured slower beside the descriptors)
 
     // colour coding (bm_colors), allocated on first use
     int* d_color_word = nullptr;    // largest vector length, float bits
