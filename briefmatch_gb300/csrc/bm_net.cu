@@ -26,6 +26,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include <cuda.h>  // CUtensorMap and its enums; the encoder is fetched through the runtime
@@ -682,17 +683,16 @@ typedef CUresult (*EncodeTiled)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, v
                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 EncodeTiled encoder()
 {
-    static EncodeTiled fn = nullptr;
-    static bool looked_up = false;
-    if (!looked_up) {
+    // looked up once per process (a function-local static initialises thread-safely)
+    static const EncodeTiled fn = []() -> EncodeTiled {
         void* f = nullptr;
         cudaDriverEntryPointQueryResult q;
         if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
                 cudaSuccess &&
             q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<EncodeTiled>(f);
-        looked_up = true;
-    }
+            return reinterpret_cast<EncodeTiled>(f);
+        return nullptr;
+    }();
     return fn;
 }
 
@@ -963,10 +963,12 @@ __global__ void __launch_bounds__(128) k_net_fused(const __grid_constant__ NetFu
 // and device; called from bm_net_create, outside any stream capture).
 cudaError_t conv_smem_optin()
 {
+    static std::mutex mu;
     static bool done[64] = {};
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lock(mu);
     if (dev < 64 && done[dev]) return cudaSuccess;
     auto set = [](const void* f, size_t bytes) {
         return cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
