@@ -686,7 +686,8 @@ __device__ __forceinline__ void trilateral_block(const float* __restrict__ U, co
     const int row0 = threadIdx.y * TRI_R;
     // NC source columns (i .. i + NC - 1) per step: NC times the independent
     // accumulation chains of a one-column walk, to keep the FMA pipe fed between the
-    // exp2s (three measured fastest; the last 2s mod 3 columns go one at a time)
+    // exp2s (three columns with the row loop unrolled four times measured fastest;
+    // the last 2s mod 3 columns go one at a time)
     auto columns = [&](int i, auto ncols) {
         constexpr int NC = decltype(ncols)::value;
         const float2* col = suv + row0 * TW + threadIdx.x + s + i;
@@ -727,7 +728,7 @@ __device__ __forceinline__ void trilateral_block(const float* __restrict__ U, co
             tap(0, c, yes{}, no{});
             tap(1, c, yes{}, no{});
         }
-#pragma unroll 2
+#pragma unroll 4
         for (int m = 2; m <= 2 * s; m++) {
 #pragma unroll
             for (int c = 0; c < NC; c++) tap(m, c, yes{}, yes{});
