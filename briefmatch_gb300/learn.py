@@ -3,9 +3,10 @@
   python -m briefmatch_gb300.learn train [--pairs 30000 --epochs 50 --out PATH]
   python -m briefmatch_gb300.learn eval [--weights PATH]
 
-Training data: seeded synthetic 512x384 pairs (briefmatch_gb300.synth); targets:
-the flow BriefMatch itself computes for each pair (the engine with 4 iterations, the
-batch API), averaged to quarter resolution.  The network is trained on the GPU by
+Training data: seeded synthetic 512x384 pairs (briefmatch_gb300.synth) -- consecutive
+pairs of sequences, independent pairs, or 512x384 windows of independent pairs of
+uneven size (`--data`); targets: the flow BriefMatch itself computes for each pair
+(the engine with 4 iterations, the batch API), averaged to quarter resolution.  The network is trained on the GPU by
 the engine's own kernels (bm_net_train_step: forward, backward and Adam on the
 tensor cores).  PyTorch only holds device buffers.
 """
@@ -26,20 +27,47 @@ TRAIN_SEED = 7_000_000
 
 
 SEQ_FRAMES = 8
+CROP_SEED = 9_000_000
+CROPS_PER_FRAME = 2
+CROP_MAX_W, CROP_MAX_H = 1920, 1080
+PAIRS_PER_GROUP = {"sequences": SEQ_FRAMES - 1, "pairs": 1, "crops": CROPS_PER_FRAME}
 
 
-def _group(g, sequences):
-    """Training group g: with `sequences`, the 7 consecutive pairs of 8-frame
-    sequence g (flow redrawn per pair, each frame warped from the previous one, as
-    in the sequence workload); else the single pair g.  Each pair is (frame0,
-    frame1, quarter-resolution truth u, v in quarter-resolution pixels)."""
+def _group(g, kind):
+    """Training group g, a list of (frame0, frame1, quarter-resolution truth u, v in
+    quarter-resolution pixels):
+
+    - "sequences": the 7 consecutive pairs of 8-frame sequence g (flow redrawn per
+      pair, each frame warped from the previous one, as in the sequence workload);
+    - "pairs": the single independent pair g;
+    - "crops": two 512x384 windows, at random places, of one independent pair whose
+      size is drawn as the batched workload draws it (width U[512,1920], height
+      U[384,1080], multiples of 4).  The synthetic flow's zoom and rotation act about
+      the frame's centre, so its motions grow with the frame: windows of large
+      frames carry the motions that large pairs have, which 512x384 frames never
+      show."""
     from briefmatch_gb300 import synth
 
-    if sequences:
+    if kind == "sequences":
         frames, flows = synth.make_sequence(TRAIN_SEED + g, TRAIN_W, TRAIN_H, SEQ_FRAMES, vmax=15.0)
         return [(frames[k], frames[k + 1], quarter(u) / 4.0, quarter(v) / 4.0) for k, (u, v) in enumerate(flows)]
-    f0, f1, u, v = synth.make_pair(TRAIN_SEED + g, TRAIN_W, TRAIN_H, vmax=15.0)
-    return [(f0, f1, quarter(u) / 4.0, quarter(v) / 4.0)]
+    if kind == "pairs":
+        f0, f1, u, v = synth.make_pair(TRAIN_SEED + g, TRAIN_W, TRAIN_H, vmax=15.0)
+        return [(f0, f1, quarter(u) / 4.0, quarter(v) / 4.0)]
+    if kind != "crops":
+        raise ValueError("unknown training data kind %r" % (kind,))
+    rng = np.random.default_rng([CROP_SEED, g])
+    W = 4 * int(rng.integers(TRAIN_W // 4, CROP_MAX_W // 4 + 1))
+    H = 4 * int(rng.integers(TRAIN_H // 4, CROP_MAX_H // 4 + 1))
+    f0, f1, u, v = synth.make_pair(CROP_SEED + g, W, H, vmax=15.0)
+    out = []
+    for _ in range(CROPS_PER_FRAME):
+        x0 = int(rng.integers(0, W - TRAIN_W + 1))
+        y0 = int(rng.integers(0, H - TRAIN_H + 1))
+        win = (slice(y0, y0 + TRAIN_H), slice(x0, x0 + TRAIN_W))
+        out.append((np.ascontiguousarray(f0[win]), np.ascontiguousarray(f1[win]), quarter(u[win]) / 4.0,
+                    quarter(v[win]) / 4.0))
+    return out
 
 
 def quarter(a):
@@ -98,10 +126,11 @@ def engine_targets(pairs, iterations=4, consistency=1.0):
     return out
 
 
-def build_set(torch, n, target_iterations, chunk=256, workers=None, sequences=True, consistency=1.0):
-    """Generate n training pairs chunk by chunk (spawn-started CPU pool, so the pool
-    never inherits a CUDA context) and keep frames and engine targets on the device.
-    Returns (frames0 [n][H][W] u8, frames1, targets [n][h4][w4][3], gt [n][h4][w4][2])."""
+def build_set(torch, n, target_iterations, chunk=256, workers=None, kind="sequences", consistency=1.0):
+    """Generate n training pairs of `kind` (see _group) chunk by chunk (spawn-started
+    CPU pool, so the pool never inherits a CUDA context) and keep frames and engine
+    targets on the device.  Returns (frames0 [n][H][W] u8, frames1, targets
+    [n][h4][w4][3], gt [n][h4][w4][2])."""
     import multiprocessing as mp
 
     from functools import partial
@@ -111,13 +140,13 @@ def build_set(torch, n, target_iterations, chunk=256, workers=None, sequences=Tr
     f1 = torch.empty_like(f0)
     tgt = torch.empty(n, TRAIN_H // 4, TRAIN_W // 4, 3, device="cuda")
     gt = np.empty((n, TRAIN_H // 4, TRAIN_W // 4, 2), np.float32)
-    per = SEQ_FRAMES - 1 if sequences else 1
+    per = PAIRS_PER_GROUP[kind]
     groups = (n + per - 1) // per
     gchunk = max(1, chunk // per)
     s = 0
     with mp.get_context("spawn").Pool(workers) as pool:
         for g0 in range(0, groups, gchunk):
-            part = [p for grp in pool.map(partial(_group, sequences=sequences), range(g0, min(groups, g0 + gchunk)))
+            part = [p for grp in pool.map(partial(_group, kind=kind), range(g0, min(groups, g0 + gchunk)))
                     for p in grp][:n - s]
             k = len(part)
             f0[s:s + k] = torch.from_numpy(np.stack([p[0] for p in part]))
@@ -187,14 +216,36 @@ def score(torch, net, f0, f1, tgt, gt, idx):
     return float(np.mean(e_tgt)), float(np.mean(e_gt)), float(np.mean(conf))
 
 
+DATA_KINDS = {
+    "sequences": "consecutive pairs of 8-frame sequences",
+    "pairs": "single pairs",
+    "crops": "512x384 windows of independent pairs of uneven size (width U[512,1920], height U[384,1080])",
+    "mixed": "half consecutive pairs of 8-frame sequences, half 512x384 windows of independent pairs of uneven "
+             "size (width U[512,1920], height U[384,1080])",
+}
+
+
 def train(args):
     import torch
 
     from briefmatch_gb300.proposal import ProposalNet
 
     t0 = time.time()
-    f0, f1, tgt, gt = build_set(torch, args.pairs, args.target_iterations, sequences=not args.single_pairs,
-                                consistency=args.consistency)
+    kind = "pairs" if args.single_pairs else args.data
+    if kind == "mixed":
+        # half sequence pairs, half windows of uneven-size independent pairs, shuffled
+        # once so that the held-out pairs cover both
+        half = args.pairs // 2
+        a = build_set(torch, half, args.target_iterations, kind="sequences", consistency=args.consistency)
+        b = build_set(torch, args.pairs - half, args.target_iterations, kind="crops", consistency=args.consistency)
+        perm = np.random.default_rng(args.seed).permutation(args.pairs)
+        tp = torch.from_numpy(perm).cuda()
+        f0, f1, tgt = (torch.cat([x, y])[tp].contiguous() for x, y in zip(a[:3], b[:3]))
+        gt = np.concatenate([a[3], b[3]])[perm]
+        del a, b
+    else:
+        f0, f1, tgt, gt = build_set(torch, args.pairs, args.target_iterations, kind=kind,
+                                    consistency=args.consistency)
     torch.cuda.synchronize()
     t_data = time.time() - t0
     n = args.pairs
@@ -210,7 +261,7 @@ def train(args):
     net.save(args.out)
     report = {"pairs": n, "heldout": nval, "size": [TRAIN_W, TRAIN_H], "epochs": args.epochs, "batch": args.batch,
               "lr": args.lr, "target_iterations": args.target_iterations, "consistency_px": args.consistency,
-              "data": "single pairs" if args.single_pairs else "consecutive pairs of 8-frame sequences",
+              "data": DATA_KINDS[kind],
               "seconds": {"data_and_targets": t_data, "train": t_train},
               "heldout_epe_vs_briefmatch_px": e_tgt, "heldout_epe_vs_truth_px": e_gt,
               "heldout_confident_fraction": conf, "loss_history": hist}
@@ -300,7 +351,8 @@ def main(argv=None):
     t.add_argument("--target-iterations", type=int, default=4)
     t.add_argument("--consistency", type=float, default=1.0,
                    help="forward-backward agreement (px) a target pixel needs; 0 keeps every pixel")
-    t.add_argument("--single-pairs", action="store_true", help="independent pairs instead of sequences")
+    t.add_argument("--data", default="sequences", choices=sorted(DATA_KINDS), help="training pairs")
+    t.add_argument("--single-pairs", action="store_true", help="independent pairs instead of sequences (--data pairs)")
     t.add_argument("--out", default=DEFAULT_WEIGHTS)
     e = sub.add_parser("eval")
     e.add_argument("--weights", default=DEFAULT_WEIGHTS)
