@@ -81,8 +81,8 @@ def parse():
                          "3 = 1920x1080 u4.9 N512 5-frame sequence; 1 and 3 run the plain engine beside the "
                          "reference's own kernels")
     ap.add_argument("--schedule", default=None,
-                    help="ITERATIONS/JFMAX[/LOCAL_STEPS] for the learned-seeded engine instead of choosing it by "
-                         "calibration")
+                    help="ITERATIONS/JFMAX[/LOCAL_STEPS[/REDUCE]] for the learned-seeded engine instead of choosing "
+                         "it by calibration")
     return ap.parse_args()
 
 
@@ -306,9 +306,11 @@ def roofline_entry(torch, kernel, n_launch, k_ms, total_k, prm, clocks):
 
 PROPOSAL_CONF = 0.5
 PIPELINED = True   # each pair's refinement overlaps the next frame (bm_set_pipelined)
-# (iterations, jfMax, local refinement steps starting at radius 2)
-SCHEDULE_CANDIDATES = tuple((it, jf, ls) for it, jf in ((1, 16), (1, 32), (1, 64), (1, 128), (1, 256), (2, 16), (2, 32),
-                                                       (2, 64)) for ls in (0, 2))
+# (iterations, jfMax, local refinement steps starting at radius 2, input reduction of
+# the network)
+SCHEDULE_CANDIDATES = tuple((it, jf, ls, 1) for it, jf in ((1, 16), (1, 32), (1, 64), (1, 128), (1, 256), (2, 16),
+                                                          (2, 32), (2, 64)) for ls in (0, 2)) + \
+    tuple((1, jf, ls, 2) for jf in (16, 32, 64, 128) for ls in (0, 2))
 
 
 def open_engine(torch, prm, pattern, stream, net=None, schedule=None):
@@ -322,6 +324,8 @@ def open_engine(torch, prm, pattern, stream, net=None, schedule=None):
         bm.set_proposal(eng, net, PROPOSAL_CONF, schedule[0], schedule[1])
         if len(schedule) > 2 and schedule[2]:
             bm.set_local_steps(eng, schedule[2], 2)
+        if len(schedule) > 3 and schedule[3] != 1:
+            bm.set_proposal_reduce(eng, schedule[3])
     if PIPELINED:
         eng.set_pipelined(True)
     return eng
@@ -465,23 +469,23 @@ def choose_schedule(torch, prm, pattern, net, stream):
     best = None
     for sch in SCHEDULE_CANDIDATES:
         ms, epe = run(open_engine(torch, prm, pattern, stream, net, sch))
-        table.append({"schedule": "seeded %d/%d/ls%d" % sch, "ms": ms, "epe": epe})
+        table.append({"schedule": "seeded %d/%d/ls%d/x%d" % sch, "ms": ms, "epe": epe})
         if epe <= plain_epe and (best is None or ms < best[1]):
             best = (sch, ms)
     return (best[0] if best else None), table
 
 
-def net_forward_timing(torch, net, d_frames, stream, reps=50):
+def net_forward_timing(torch, net, d_frames, stream, reps=50, reduce=1):
     """Device time of the proposal network's input preparation + forward pass for one
-    1024x436 pair (quarter resolution 256x109), and its tensor-core rate."""
+    1024x436 pair (256x109 cells of 4 pixels with reduce 1), and its tensor-core rate."""
     from briefmatch_gb300.proposal import flops_per_pixel
 
-    h4, w4 = H // 4, W // 4
+    h4, w4 = H // reduce // 4, W // reduce // 4
     out = torch.empty(1, h4, w4, 3, device="cuda")
     st = stream.cuda_stream
 
     def once():
-        net.prepare(0, d_frames[0].data_ptr(), d_frames[1].data_ptr(), W, H, st)
+        net.prepare(0, d_frames[0].data_ptr(), d_frames[1].data_ptr(), W, H, st, reduce=reduce)
         net.forward(1, h4, w4, out.data_ptr(), st)
 
     for _ in range(5):
@@ -497,7 +501,8 @@ def net_forward_timing(torch, net, d_frames, stream, reps=50):
     flops = flops_per_pixel() * h4 * w4
     return {"ms_per_pair": ms, "gflop_per_pair": flops / 1e9, "tflop_s": flops / (ms * 1e-3) / 1e12,
             "path": {2: "tcgen05, one cooperative launch", 1: "tcgen05, a launch per layer", 0: "mma.sync"}[net.umma],
-            "note": "input preparation + 6 conv layers, 1 pair, back to back"}
+            "note": "input preparation + 6 conv layers, 1 pair, back to back", "reduce": reduce,
+            "cells": [h4, w4]}
 
 
 def run_engine(args, torch, world, rank):
@@ -529,7 +534,7 @@ def run_engine(args, torch, world, rank):
         net = learn.load_net(learn.DEFAULT_WEIGHTS, 1, H // 4, W // 4)
         if args.schedule:
             sch = tuple(int(x) for x in args.schedule.split("/"))
-            sch, table = (sch + (0,))[:3], "given on the command line"
+            sch, table = (sch + (0, 1)[len(sch) - 2:])[:4], "given on the command line"
         else:
             sch, table = choose_schedule(torch, prm, pattern, net, stream)
         # the network's forward on both tensor-core paths (tcgen05 is the engine's)
@@ -537,7 +542,7 @@ def run_engine(args, torch, world, rank):
         default_mode = net.umma
         for path, mode in (("mma_sync", 0), ("tcgen05_fused", 2), ("tcgen05_per_layer", 1)):
             net.set_umma(mode)
-            nf[path] = net_forward_timing(torch, net, d_frames, stream)
+            nf[path] = net_forward_timing(torch, net, d_frames, stream, reduce=sch[3] if sch else 1)
         net.set_umma(default_mode)  # the engines below run the network's default path
         net.check(stream.cuda_stream)
         nf["tcgen05_fused"]["ctas"] = net.fused_ctas
@@ -547,7 +552,7 @@ def run_engine(args, torch, world, rank):
         if sch is not None:
             seng = open_engine(torch, prm, pattern, stream, net, sch)
             rl = measure(args, torch, world, seng, d_frames, flows, stream, flush)
-            learned.update({"schedule": {"iterations": sch[0], "jfMax": sch[1], "local_steps": sch[2]},
+            learned.update({"schedule": {"iterations": sch[0], "jfMax": sch[1], "local_steps": sch[2], "reduce": sch[3]},
                             "value": rl["value"],
                             "ms_per_step": rl["ms_per_step"], "epe_mean": float(np.mean(rl["epe"])),
                             "speedup_vs_plain": rp["ms_per_step"] / rl["ms_per_step"],
@@ -674,7 +679,12 @@ def make_batch_workload(pairs, seed=None):
     return sizes, data
 
 
-BATCH_CANDIDATES = ((2, 64, 0), (2, 64, 2), (2, 32, 2), (1, 256, 2), (1, 128, 2))
+# seeded batch schedules: (input reduction of the network, iterations, jfMax, local
+# steps).  Fresh pairs start from the zero field, and the network's motions on frames
+# much larger than its 512x384 training frames exceed what it saw: reduction 2
+# (cells of 8 pixels) brings them back into its range
+BATCH_CANDIDATES = ((1, 2, 64, 0), (1, 2, 64, 2), (1, 1, 128, 2), (2, 2, 64, 0), (2, 1, 128, 0), (2, 1, 64, 0),
+                    (2, 1, 32, 0), (2, 1, 16, 0), (2, 1, 64, 2), (2, 1, 32, 2), (2, 1, 16, 2))
 
 
 def batch_step_ms_epe(torch, b, data, stream, reps):
@@ -696,9 +706,9 @@ def batch_step_ms_epe(torch, b, data, stream, reps):
 
 
 def choose_batch_schedule(torch, net, stream, pairs=16):
-    """The fastest seeded (iterations, jfMax, local steps) whose mean EPE on a separate
-    calibration batch (other seeds of the same uneven-size generator) is at most the
-    plain batch's there."""
+    """The fastest seeded (reduction, iterations, jfMax, local steps) whose mean EPE on
+    a separate calibration batch (other seeds of the same uneven-size generator) is at
+    most the plain batch's there."""
     import briefmatch_gb300 as bm
     from briefmatch_gb300.proposal import ProposalNet
 
@@ -714,11 +724,12 @@ def choose_batch_schedule(torch, net, stream, pairs=16):
     bnet.set_params(net.params())
     best = None
     for sch in BATCH_CANDIDATES:
-        b.set_proposal(bnet, PROPOSAL_CONF, sch[0], sch[1])
-        b.set_local_steps(sch[2], 2)
+        b.set_proposal(bnet, PROPOSAL_CONF, sch[1], sch[2])
+        b.set_proposal_reduce(sch[0])
+        b.set_local_steps(sch[3], 2)
         b.set_schedule(per_pair=1, use_graph=1, streams=2)
         ms, epe = batch_step_ms_epe(torch, b, data, stream, 2)
-        table.append({"schedule": "seeded %d/%d/ls%d" % sch, "ms": ms, "epe": epe})
+        table.append({"schedule": "seeded x%d %d/%d/ls%d" % sch, "ms": ms, "epe": epe})
         if epe <= plain_epe and (best is None or ms < best[1]):
             best = (sch, ms)
     b.set_proposal(None)
@@ -760,6 +771,16 @@ def run_batched(args, torch, sizes, data, net=None, schedule=None):
     flows = b.read_flows()
     epe = float(np.mean([np.mean(np.hypot(f[0] - d[2], f[1] - d[3])) for f, d in zip(flows, data)]))
     sched = b.schedule()
+    # the same pairs with almost no matching (one iteration, jump maximum 1: a single
+    # level fused with the random search) on the plain batch's schedule: the cost of
+    # every stage that a proposal cannot shorten, so batch_ms / floor_ms bounds the gain
+    # of any seeded schedule on this workload
+    fb = bm.Batch([bm.BMParams.derive(w, h, UP, UP, N=NBITS, iterations=1, jfMax=1) for w, h in sizes])
+    fb.set_stream(stream.cuda_stream)
+    fb.load_frames(d_packed.data_ptr(), on_device=True)
+    fb.set_schedule(**sched)
+    floor_ms, floor_epe = batch_step_ms_epe(torch, fb, data, stream, max(1, args.steps))
+    fb.close()
     learned = None
     calibration = None
     if net is not None:
@@ -769,8 +790,9 @@ def run_batched(args, torch, sizes, data, net=None, schedule=None):
 
         bnet = ProposalNet(1, max(h for _, h in sizes) // 4, max(w for w, _ in sizes) // 4)
         bnet.set_params(net.params())
-        b.set_proposal(bnet, PROPOSAL_CONF, schedule[0], schedule[1])
-        b.set_local_steps(schedule[2], 2)
+        b.set_proposal(bnet, PROPOSAL_CONF, schedule[1], schedule[2])
+        b.set_proposal_reduce(schedule[0])
+        b.set_local_steps(schedule[3], 2)
         lrep = b.autotune(None, reps=2)
         for _ in range(args.warmup):
             b.run()
@@ -784,7 +806,8 @@ def run_batched(args, torch, sizes, data, net=None, schedule=None):
         lms = sum(s0.elapsed_time(s1) for s0, s1 in ev) / args.steps
         lflows = b.read_flows()
         lepe = float(np.mean([np.mean(np.hypot(f[0] - d[2], f[1] - d[3])) for f, d in zip(lflows, data)]))
-        learned = {"schedule": {"iterations": schedule[0], "jfMax": schedule[1], "local_steps": schedule[2]},
+        learned = {"schedule": {"reduce": schedule[0], "iterations": schedule[1], "jfMax": schedule[2],
+                                "local_steps": schedule[3]},
                    "value": out_px / (lms * 1e-3) / 1e6,
                    "ms_per_step": lms, "epe_mean": lepe, "speedup_vs_plain_batch": batch_ms / lms,
                    "autotune": lrep, "batch_schedule": b.schedule(), "calibration": calibration}
@@ -830,6 +853,8 @@ def run_batched(args, torch, sizes, data, net=None, schedule=None):
         "sequential_value": out_px / (seq_ms * 1e-3) / 1e6, "sequential_ms_per_step": seq_ms,
         "speedup_vs_sequential": seq_ms / batch_ms,
         "schedule": sched, "autotune": report, "epe_mean": epe,
+        "matching_floor": {"what": "1 iteration, jump maximum 1, no proposal, plain schedule", "ms_per_step": floor_ms,
+                           "epe_mean": floor_epe, "ceiling_vs_plain_batch": batch_ms / floor_ms},
         "learned": dict(learned, speedup_vs_plain_sequential=seq_ms / learned["ms_per_step"]) if learned else
         ({"schedule": None, "calibration": calibration} if calibration else None),
     }

@@ -108,12 +108,14 @@ def _declare(lib):
         "bm_profile_read": (c.c_int, [c.c_void_p, c.c_void_p, c.c_uint32, P(c.c_uint32)]),
         "bm_set_proposal": (c.c_int, [c.c_void_p, c.c_void_p, c.c_float, c.c_uint32, c.c_uint32]),
         "bm_set_proposal_stream": (c.c_int, [c.c_void_p, c.c_int]),
+        "bm_set_proposal_reduce": (c.c_int, [c.c_void_p, c.c_uint32]),
         "bm_set_pipelined": (c.c_int, [c.c_void_p, c.c_int]),
         "bm_set_local_steps": (c.c_int, [c.c_void_p, c.c_uint32, c.c_uint32]),
         "bm_local_step": (c.c_int, [c.c_void_p, c.c_uint32]),
         "bm_batch_set_local_steps": (c.c_int, [c.c_void_p, c.c_uint32, c.c_uint32]),
         "bm_join": (c.c_int, [c.c_void_p]),
         "bm_batch_set_proposal": (c.c_int, [c.c_void_p, c.c_void_p, c.c_float, c.c_uint32, c.c_uint32]),
+        "bm_batch_set_proposal_reduce": (c.c_int, [c.c_void_p, c.c_uint32]),
         "bm_seed": (c.c_int, [c.c_void_p, c.c_int, c.c_void_p, c.c_uint32, c.c_uint32, c.c_float]),
         "bm_refine_noalloc": (c.c_int, [c.c_void_p, c.c_void_p, c.c_void_p, c.c_void_p, c.c_void_p, c.c_uint32,
                                         c.c_uint32, c.c_uint32, c.c_float, c.c_float, c.c_float, c.c_void_p]),
@@ -534,6 +536,10 @@ class Batch:
         check(lib().bm_batch_set_proposal(self._b, net.handle if net is not None else None, conf_threshold,
                                           iterations, jf_max))
 
+    def set_proposal_reduce(self, reduce):
+        """The network's input reduction for every pair (bm_batch_set_proposal_reduce)."""
+        check(lib().bm_batch_set_proposal_reduce(self._b, reduce))
+
 
 def set_proposal_stream(engine, side=True):
     """Whether the context runs the proposal network on its own side stream or on the
@@ -545,6 +551,12 @@ def set_proposal(engine, net, conf_threshold=0.5, iterations=1, jf_max=16):
     """Attach a ProposalNet (or None) to a BriefMatch context (bm_set_proposal)."""
     check(lib().bm_set_proposal(engine.ctx, net.handle if net is not None else None, conf_threshold, iterations,
                                 jf_max))
+
+
+def set_proposal_reduce(engine, reduce):
+    """Cells of 4 * reduce input pixels for the context's proposal network: the
+    network sees the frames reduced by `reduce` (bm_set_proposal_reduce)."""
+    check(lib().bm_set_proposal_reduce(engine.ctx, reduce))
 
 
 def set_local_steps(engine, count, first_radius=2):

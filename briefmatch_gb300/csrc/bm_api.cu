@@ -117,8 +117,11 @@ struct bm_ctx {
     bm_net* net = nullptr;
     float net_logit_min = 0.0f;
     uint32_t net_iterations = 0, net_jfMax = 0;
+    uint32_t net_reduce = 1;   // bm_set_proposal_reduce: cells of 4 * net_reduce input pixels
     uint32_t local_steps = 0, local_radius = 1;   // bm_set_local_steps
     float* d_pred = nullptr;   // [h4][w4][3]
+    uint32_t net_w4() const { return prm.sx_in / net_reduce / 4; }
+    uint32_t net_h4() const { return prm.sy_in / net_reduce / 4; }
     // with bm_set_proposal_stream(ctx, 1) the network runs on a side stream,
     // concurrently with the frame's up-sampling and descriptors: it starts once both
     // 8-bit frames are on the device (ev_u8) and the seed waits for it (ev_net)
@@ -336,8 +339,10 @@ bm_status match_impl(bm_ctx* c, const float* d_im2, bool seeded, bool padded = f
     const int first = (c->first_match || !p.tInit) ? 1 : 0;
     uint32_t iterations = p.iterations, jfMax = p.jfMax;
     if (seeded) {
-        const int w4 = (int)p.sx_in / 4, h4 = (int)p.sy_in / 4;
-        const float scx = 4.0f * (float)p.sx / (float)p.sx_in, scy = 4.0f * (float)p.sy / (float)p.sy_in;
+        // a cell covers 4 * net_reduce input pixels; its vector is in those units
+        const int w4 = (int)c->net_w4(), h4 = (int)c->net_h4();
+        const float cell = 4.0f * (float)c->net_reduce;
+        const float scx = cell * (float)p.sx / (float)p.sx_in, scy = cell * (float)p.sy / (float)p.sy_in;
         if (c->net_pending) {  // the proposal computed on the side stream
             BM_CUDA(cudaStreamWaitEvent(c->stream, c->ev_net, 0));
             c->net_pending = false;
@@ -920,6 +925,17 @@ bm_status bm_set_proposal(bm_ctx* c, bm_net* net, float conf_threshold, uint32_t
     return BM_OK;
 }
 
+bm_status bm_set_proposal_reduce(bm_ctx* c, uint32_t reduce)
+{
+    if (check_ctx(c)) return BM_ERR_INVALID;
+    if (reduce != 1 && reduce != 2 && reduce != 4)
+        return fail(BM_ERR_INVALID, "bm_set_proposal_reduce: reduce must be 1, 2 or 4");
+    if (c->prm.sx_in < 4 * reduce || c->prm.sy_in < 4 * reduce)
+        return fail(BM_ERR_LIMIT, "bm_set_proposal_reduce: frame too small");
+    c->net_reduce = reduce;
+    return BM_OK;
+}
+
 bm_status bm_set_proposal_stream(bm_ctx* c, int side)
 {
     if (check_ctx(c)) return BM_ERR_INVALID;
@@ -1023,10 +1039,11 @@ bm_status bm_frame(bm_ctx* c, const uint8_t* frame, int frame_on_device, float* 
     if (seeded && c->net_side) {
         // the proposal network on its side stream, from the previous and this frame,
         // while this stream up-samples and describes the frame; match_impl's seed waits
-        const uint32_t w4 = p.sx_in / 4, h4 = p.sy_in / 4;
+        const uint32_t w4 = c->net_w4(), h4 = c->net_h4();
         BM_CUDA(cudaEventRecord(c->ev_u8, c->stream));
         BM_CUDA(cudaStreamWaitEvent(c->net_stream, c->ev_u8, 0));
-        bm_status nst = bm_net_prepare(c->net, 0, c->d_u8[prev], d_u8, p.sx_in, p.sy_in, c->net_stream);
+        bm_status nst = bm_net_prepare_reduced(c->net, 0, c->d_u8[prev], d_u8, p.sx_in, p.sy_in, c->net_reduce,
+                                               c->net_stream);
         if (nst == BM_OK) nst = bm_net_forward(c->net, 1, h4, w4, c->d_pred, c->net_stream);
         if (nst != BM_OK) return nst;
         BM_CUDA(cudaEventRecord(c->ev_net, c->net_stream));
@@ -1055,8 +1072,8 @@ bm_status bm_frame(bm_ctx* c, const uint8_t* frame, int frame_on_device, float* 
         c->primed = true;
     } else {
         if (seeded && !c->net_side) {  // the network on the context stream, after up-sampling
-            const uint32_t w4 = p.sx_in / 4, h4 = p.sy_in / 4;
-            st = bm_net_prepare(c->net, 0, c->d_u8[prev], d_u8, p.sx_in, p.sy_in, c->stream);
+            const uint32_t w4 = c->net_w4(), h4 = c->net_h4();
+            st = bm_net_prepare_reduced(c->net, 0, c->d_u8[prev], d_u8, p.sx_in, p.sy_in, c->net_reduce, c->stream);
             if (st == BM_OK) st = bm_net_forward(c->net, 1, h4, w4, c->d_pred, c->stream);
             if (st != BM_OK) return st;
             c->launches += 7;

@@ -315,6 +315,7 @@ struct bm_batch {
     bm_net* net = nullptr;
     float net_logit_min = 0.0f;
     uint32_t net_iterations = 0, net_jfMax = 0;
+    uint32_t net_reduce = 1;   // bm_batch_set_proposal_reduce: cells of 4 * net_reduce input pixels
     uint32_t local_steps = 0, local_radius = 1;   // bm_batch_set_local_steps
     float* d_pred = nullptr;   // [h4][w4][3] of the pair being seeded (pairs run in stream order)
     // concurrent branches of the per-pair schedule (bm_batch_schedule.streams):
@@ -443,11 +444,14 @@ bm_status enqueue_pair(bm_batch* b, const bm_batch_schedule& s, int j, cudaStrea
     uint32_t iterations = b->iterations, jfMax = b->jfMax;
     if (net) {
         // the proposal for this pair, then the seeded initialisation (bm_seed's rule)
-        const uint32_t w4 = (uint32_t)d.sx_in / 4, h4 = (uint32_t)d.sy_in / 4;
-        bm_status nst = bm_net_prepare(net, 0, d.frame[0], d.frame[1], (uint32_t)d.sx_in, (uint32_t)d.sy_in, st);
+        const uint32_t red = b->net_reduce;
+        const uint32_t w4 = (uint32_t)d.sx_in / red / 4, h4 = (uint32_t)d.sy_in / red / 4;
+        bm_status nst = bm_net_prepare_reduced(net, 0, d.frame[0], d.frame[1], (uint32_t)d.sx_in, (uint32_t)d.sy_in, red,
+                                               st);
         if (nst == BM_OK) nst = bm_net_forward(net, 1, h4, w4, d_pred, st);
         if (nst != BM_OK) return nst;
-        const float scx = 4.0f * (float)d.sx / (float)d.sx_in, scy = 4.0f * (float)d.sy / (float)d.sy_in;
+        const float cell = 4.0f * (float)red;
+        const float scx = cell * (float)d.sx / (float)d.sx_in, scy = cell * (float)d.sy / (float)d.sy_in;
         BB_CUDA(seed_field(d.F[0], d.F[1], d.flow[cur], d.flow[cur ^ 1], d.cost, d.sx, d.sy, (int)b->nsp, 1, d_pred,
                            (int)w4, (int)h4, scx, scy, b->net_logit_min, st));
         iterations = b->net_iterations;
@@ -766,7 +770,9 @@ std::string shape_key(const bm_batch* b)
     std::ostringstream ss;
     ss << prop.name << "|pairs=" << b->count << "|N=" << b->N << "|it=" << b->iterations << "|jf=" << b->jfMax
        << "|upMpx=" << (px + 500000) / 1000000;
-    if (b->net) ss << "|seeded=" << b->net_iterations << "/" << b->net_jfMax << "/ls" << b->local_steps << "r" << b->local_radius;
+    if (b->net)
+        ss << "|seeded=" << b->net_iterations << "/" << b->net_jfMax << "/ls" << b->local_steps << "r" << b->local_radius
+           << "/x" << b->net_reduce;
     return ss.str();
 }
 
@@ -1215,6 +1221,20 @@ bm_status bm_batch_set_proposal(bm_batch* b, bm_net* net, float conf_threshold, 
     b->net_jfMax = jfMax;
     destroy_graph(b);
     if (net && b->sched.streams > 1) return ensure_branches(b, (int)b->sched.streams);
+    return BM_OK;
+}
+
+bm_status bm_batch_set_proposal_reduce(bm_batch* b, uint32_t reduce)
+{
+    if (!b) return bfail(BM_ERR_INVALID, "null batch");
+    if (reduce != 1 && reduce != 2 && reduce != 4)
+        return bfail(BM_ERR_INVALID, "bm_batch_set_proposal_reduce: reduce must be 1, 2 or 4");
+    for (const auto& p : b->prm)
+        if (p.sx_in < 4 * reduce || p.sy_in < 4 * reduce)
+            return bfail(BM_ERR_LIMIT, "bm_batch_set_proposal_reduce: frame too small");
+    if (b->stream) BB_CUDA(cudaStreamSynchronize(b->stream));
+    b->net_reduce = reduce;
+    destroy_graph(b);
     return BM_OK;
 }
 

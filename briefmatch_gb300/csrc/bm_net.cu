@@ -311,6 +311,42 @@ __global__ void k_net_input(const uint8_t* __restrict__ f0, const uint8_t* __res
     for (int q = 0; q < 4; q++) o[q] = make_uint4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
 }
 
+// The same from frames reduced by `red` (2 or 4, lg = log2(red)): the cell (x, y)
+// covers the 4x4 reduced pixels (4x + i, 4y + j), each the mean of the red x red
+// input pixels it stands for, rounded half to even to an 8-bit value (w4 = (W / red)
+// / 4, h4 = (H / red) / 4, so every block lies inside the frame).
+__global__ void k_net_input_reduced(const uint8_t* __restrict__ f0, const uint8_t* __restrict__ f1, int W,
+                                    __nv_bfloat16* __restrict__ out, int w4, int h4, int red, int lg)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= w4 || y >= h4) return;
+    const uint32_t sh = 2u * (uint32_t)lg, half = 1u << (sh - 1), mask = (1u << sh) - 1u;
+    uint32_t v[16];
+#pragma unroll
+    for (int f = 0; f < 2; f++) {
+        const uint8_t* src = f ? f1 : f0;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            float val[4];
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const uint8_t* p = src + (size_t)((4 * y + j) * red) * W + (size_t)(4 * x + i) * red;
+                uint32_t sum = 0;
+                for (int a = 0; a < red; a++)
+                    for (int b = 0; b < red; b++) sum += __ldg(p + (size_t)a * W + b);
+                const uint32_t q = sum >> sh, rem = sum & mask;
+                const uint32_t m = q + ((rem > half || (rem == half && (q & 1u))) ? 1u : 0u);
+                val[i] = (float)m / 127.5f - 1.0f;
+            }
+            v[f * 8 + j * 2] = pack_bf16(val[0], val[1]);
+            v[f * 8 + j * 2 + 1] = pack_bf16(val[2], val[3]);
+        }
+    }
+    uint4* o = reinterpret_cast<uint4*>(out + ((size_t)y * w4 + x) * NIN);
+#pragma unroll
+    for (int q = 0; q < 4; q++) o[q] = make_uint4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+}
+
 // Loss of the head against BriefMatch's flow: smooth-L1 on (u, v) in quarter
 // resolution pixels and binary cross-entropy of the confidence against "the
 // predicted vector is within tau of the target", averaged over valid pixels.
@@ -1273,19 +1309,30 @@ bm_status bm_net_get_params(bm_net* n, float* h_params, size_t count)
     return BM_OK;
 }
 
-// Network input of image b from two 8-bit frames W x H (device).
-bm_status bm_net_prepare(bm_net* n, uint32_t b, const uint8_t* d_f0, const uint8_t* d_f1, uint32_t W, uint32_t H,
-                         void* stream)
+// Network input of image b from two 8-bit frames W x H (device), reduced by `reduce`.
+bm_status bm_net_prepare_reduced(bm_net* n, uint32_t b, const uint8_t* d_f0, const uint8_t* d_f1, uint32_t W,
+                                 uint32_t H, uint32_t reduce, void* stream)
 {
     if (!n || !d_f0 || !d_f1) return nfail(BM_ERR_INVALID, "bm_net_prepare: null argument");
-    const uint32_t w4 = W / 4, h4 = H / 4;
+    if (reduce != 1 && reduce != 2 && reduce != 4) return nfail(BM_ERR_INVALID, "bm_net_prepare: reduce must be 1, 2 or 4");
+    const uint32_t w4 = W / reduce / 4, h4 = H / reduce / 4;
     if (b >= n->maxB || (size_t)w4 * h4 > (size_t)n->maxh * n->maxw || w4 == 0 || h4 == 0)
         return nfail(BM_ERR_LIMIT, "bm_net_prepare: beyond the network's buffers");
     dim3 blk(32, 8), g((w4 + 31) / 32, (h4 + 7) / 8);
-    k_net_input<<<g, blk, 0, (cudaStream_t)stream>>>(d_f0, d_f1, (int)W, (int)H, n->d_in + (size_t)b * h4 * w4 * NIN,
-                                                     (int)w4, (int)h4);
+    __nv_bfloat16* dst = n->d_in + (size_t)b * h4 * w4 * NIN;
+    if (reduce == 1)
+        k_net_input<<<g, blk, 0, (cudaStream_t)stream>>>(d_f0, d_f1, (int)W, (int)H, dst, (int)w4, (int)h4);
+    else
+        k_net_input_reduced<<<g, blk, 0, (cudaStream_t)stream>>>(d_f0, d_f1, (int)W, dst, (int)w4, (int)h4, (int)reduce,
+                                                                  reduce == 2 ? 1 : 2);
     BN_CUDA(cudaGetLastError());
     return BM_OK;
+}
+
+bm_status bm_net_prepare(bm_net* n, uint32_t b, const uint8_t* d_f0, const uint8_t* d_f1, uint32_t W, uint32_t H,
+                         void* stream)
+{
+    return bm_net_prepare_reduced(n, b, d_f0, d_f1, W, H, 1, stream);
 }
 
 // Raw network input (bf16 NHWC, 32 channels) for tests.

@@ -28,6 +28,8 @@ def _declare():
         "bm_net_set_params": (c.c_int, [c.c_void_p, c.c_void_p, c.c_size_t]),
         "bm_net_get_params": (c.c_int, [c.c_void_p, c.c_void_p, c.c_size_t]),
         "bm_net_prepare": (c.c_int, [c.c_void_p, c.c_uint32, c.c_void_p, c.c_void_p, c.c_uint32, c.c_uint32, c.c_void_p]),
+        "bm_net_prepare_reduced": (c.c_int, [c.c_void_p, c.c_uint32, c.c_void_p, c.c_void_p, c.c_uint32, c.c_uint32,
+                                             c.c_uint32, c.c_void_p]),
         "bm_net_set_input": (c.c_int, [c.c_void_p, c.c_void_p, c.c_uint32, c.c_uint32, c.c_uint32, c.c_void_p]),
         "bm_net_forward": (c.c_int, [c.c_void_p, c.c_uint32, c.c_uint32, c.c_uint32, c.c_void_p, c.c_void_p]),
         "bm_net_train_step": (c.c_int, [c.c_void_p, c.c_uint32, c.c_uint32, c.c_uint32, c.c_void_p, c.c_float,
@@ -95,9 +97,11 @@ class ProposalNet:
     def load(self, path):
         self.set_params(np.fromfile(path, np.float32))
 
-    def prepare(self, b, d_f0, d_f1, W, H, stream=0):
-        check(lib().bm_net_prepare(self._n, b, ctypes.c_void_p(d_f0), ctypes.c_void_p(d_f1), W, H,
-                                   ctypes.c_void_p(stream)))
+    def prepare(self, b, d_f0, d_f1, W, H, stream=0, reduce=1):
+        """Input image b from two 8-bit W x H device frames, reduced by `reduce`
+        (bm_net_prepare_reduced): ((W // reduce) // 4) x ((H // reduce) // 4) cells."""
+        check(lib().bm_net_prepare_reduced(self._n, b, ctypes.c_void_p(d_f0), ctypes.c_void_p(d_f1), W, H, reduce,
+                                           ctypes.c_void_p(stream)))
 
     def set_input(self, d_in_bf16, B, h, w, stream=0):
         check(lib().bm_net_set_input(self._n, ctypes.c_void_p(d_in_bf16), B, h, w, ctypes.c_void_p(stream)))

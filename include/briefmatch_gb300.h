@@ -278,6 +278,8 @@ bm_status bm_batch_autotune(bm_batch* b, const char* cache_path, int reps, char*
  * used on another stream while the batch runs. */
 typedef struct bm_net bm_net;
 bm_status bm_batch_set_proposal(bm_batch* b, bm_net* net, float conf_threshold, uint32_t iterations, uint32_t jfMax);
+/* The network's input reduction for every pair (bm_set_proposal_reduce); 1 by default. */
+bm_status bm_batch_set_proposal_reduce(bm_batch* b, uint32_t reduce);
 /* Local refinement steps after each pair's seeded initialisation (bm_set_local_steps). */
 bm_status bm_batch_set_local_steps(bm_batch* b, uint32_t count, uint32_t first_radius);
 
@@ -321,6 +323,12 @@ bm_status bm_net_get_params(bm_net* n, float* h_params, size_t count);
  * pixel (4x + i, 4y + j) of frame 0 scaled to [-1, 1]; channels 16..31: frame 1). */
 bm_status bm_net_prepare(bm_net* n, uint32_t b, const uint8_t* d_f0, const uint8_t* d_f1, uint32_t W, uint32_t H,
                          void* stream);
+/* The same from the frames reduced by `reduce` (1, 2 or 4): reduced pixel (X, Y) is
+ * the mean of input pixels (reduce*X + a, reduce*Y + b), a, b < reduce, rounded half
+ * to even to an 8-bit value; the image is ((W / reduce) / 4) x ((H / reduce) / 4)
+ * cells, each covering 4 * reduce input pixels.  reduce 1 is bm_net_prepare. */
+bm_status bm_net_prepare_reduced(bm_net* n, uint32_t b, const uint8_t* d_f0, const uint8_t* d_f1, uint32_t W,
+                                 uint32_t H, uint32_t reduce, void* stream);
 /* Raw input: B images h x w, bf16 NHWC with 32 channels. */
 bm_status bm_net_set_input(bm_net* n, const uint16_t* d_in, uint32_t B, uint32_t h, uint32_t w, void* stream);
 /* Forward; d_out (may be NULL) receives [B][h][w][3] floats (u, v, confidence logit). */
@@ -364,6 +372,14 @@ bm_status bm_set_proposal(bm_ctx* ctx, bm_net* net, float conf_threshold, uint32
  * 1.5 % slower per step (its kernels take shared memory from the L1-bound descriptor
  * kernel running beside them). */
 bm_status bm_set_proposal_stream(bm_ctx* ctx, int side);
+/* No counterpart in the reference.  The network of bm_set_proposal sees the frames
+ * reduced by `reduce` (1, the default, 2 or 4; bm_net_prepare_reduced): a cell covers
+ * 4 * reduce input pixels and its predicted vector is in those units, which the seed
+ * scales accordingly.  The network was trained on 512x384 frames; on larger frames,
+ * whose motions exceed what it saw, a reduced input brings them back into its range
+ * (on uneven 512-1920 px pairs: proposal 2.0 -> 1.0 px from the truth with reduce 2).
+ * BM_ERR_LIMIT if a frame side is below 4 * reduce. */
+bm_status bm_set_proposal_reduce(bm_ctx* ctx, uint32_t reduce);
 
 /* Seeded initialisation (the stage entry point): each up-sampled pixel first takes
  * the plain initialisation (CUDA_initialize semantics: zero vector, or the temporal

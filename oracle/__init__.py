@@ -322,9 +322,10 @@ class Sequence:
     to take libm-vs-fast-math Lanczos differences out of a comparison);
     ``normals_fn(call, n)`` supplies the random-search normals of call ``call``;
     ``nn`` the device's down-sampling index tables (see ``downsample``).
-    ``proposal`` = (pred_fn, logit_min, iterations, jf_max[, local_radii])
+    ``proposal`` = (pred_fn, logit_min, iterations, jf_max[, local_radii[, reduce]])
     switches matching to the seeded schedule: pred_fn(prev_u8, cur_u8) gives the
-    [h4][w4][3] quarter-resolution proposal, ``seed`` replaces the plain
+    [h4][w4][3] proposal on cells of 4 * reduce input pixels (h4 = sy_in // reduce
+    // 4, w4 likewise; reduce 1 by default), ``seed`` replaces the plain
     initialisation, one ``local_step`` follows per radius in local_radii, and the
     proposal's iteration count and jump maximum replace the parameters' (jf_max 0
     keeps them)."""
@@ -363,11 +364,13 @@ class Sequence:
             else:
                 pred_fn, logit_min, it, jf = self.proposal[:4]
                 radii = self.proposal[4] if len(self.proposal) > 4 else ()
+                red = self.proposal[5] if len(self.proposal) > 5 else 1
                 jf = jf or p["jfMax"]
-                w4, h4 = sxi // 4, syi // 4
+                # bm_api.cu match_impl: a cell covers 4 * reduce input pixels
+                w4, h4 = sxi // red // 4, syi // red // 4
                 f32 = np.float32
-                scx = f32(4.0) * f32(sx) / f32(sxi)
-                scy = f32(4.0) * f32(sy) / f32(syi)
+                scx = f32(4.0 * red) * f32(sx) / f32(sxi)
+                scy = f32(4.0 * red) * f32(sy) / f32(syi)
                 pred = pred_fn(self.prev_u8, frame_u8)
                 NX, NY, H = seed(self.F1, F2, sx, sy, N, first, pred, w4, h4, scx, scy, logit_min, self.NX, self.NY)
                 for r in radii:

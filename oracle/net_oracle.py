@@ -21,6 +21,33 @@ def bf16(x):
     return r.astype(np.uint32).view(np.float32).reshape(np.shape(x))
 
 
+def reduce_frame(f, r):
+    """An 8-bit frame reduced by r (bm_net.cu k_net_input_reduced): pixel (X, Y) is the
+    mean of the r x r input pixels (r*X + a, r*Y + b), rounded half to even; a ragged
+    right or bottom edge is dropped."""
+    f = np.asarray(f)
+    if r == 1:
+        return f.astype(np.uint8)
+    h, w = f.shape[0] // r, f.shape[1] // r
+    s = f[:h * r, :w * r].astype(np.int64).reshape(h, r, w, r).sum(axis=(1, 3))
+    return np.rint(s / float(r * r)).astype(np.uint8)
+
+
+def net_input(f0, f1, reduce=1):
+    """The network input of bm_net_prepare_reduced (bm_net.cu k_net_input /
+    k_net_input_reduced) as float32 before BF16 rounding, [h4][w4][32]: channel
+    4*j + i of cell (x, y) is pixel (4x + i, 4y + j) of reduced frame 0 scaled to
+    [-1, 1], channels 16..31 the same for frame 1; h4 x w4 = (H // reduce // 4) x
+    (W // reduce // 4)."""
+    out = []
+    for f in (f0, f1):
+        g = reduce_frame(f, reduce)
+        h4, w4 = g.shape[0] // 4, g.shape[1] // 4
+        c = g[:h4 * 4, :w4 * 4].reshape(h4, 4, w4, 4).transpose(0, 2, 1, 3).reshape(h4, w4, 16)
+        out.append(c.astype(np.float32) / np.float32(127.5) - np.float32(1.0))
+    return np.concatenate(out, axis=2)
+
+
 def unpack(params):
     out, k = [], 0
     for ci, co in zip(CIN, COUT):

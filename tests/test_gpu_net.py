@@ -15,6 +15,7 @@ torch = pytest.importorskip("torch")
 if not torch.cuda.is_available():
     pytest.skip("no GPU", allow_module_level=True)
 
+import briefmatch_gb300 as bm  # noqa: E402
 from briefmatch_gb300.proposal import ProposalNet, param_count  # noqa: E402
 
 
@@ -80,6 +81,55 @@ def test_input_preparation():
     want_u = np.maximum(bf(f0[0::4, 0::4]), 0)
     want_v = np.maximum(bf(f1[3::4, 3::4]), 0)
     assert np.array_equal(o[..., 0], want_u) and np.array_equal(o[..., 1], want_v)
+
+
+@pytest.mark.parametrize("reduce,W,H", [(1, 40, 24), (2, 70, 45), (4, 70, 45)])
+def test_input_preparation_reduced(reduce, W, H):
+    """bm_net_prepare_reduced against net_oracle.net_input, every channel and sign: a
+    probe network passes input channel c of both frames through the centre taps as
+    relu(x) - relu(-x) = x, so the head outputs the BF16 input values exactly."""
+    rng = np.random.default_rng(10 + reduce)
+    f0 = rng.integers(0, 256, (H, W), dtype=np.uint8)
+    f1 = rng.integers(0, 256, (H, W), dtype=np.uint8)
+    want = net_oracle.bf16(net_oracle.net_input(f0, f1, reduce))
+    h4, w4 = H // reduce // 4, W // reduce // 4
+    assert want.shape == (h4, w4, 32)
+    net = ProposalNet(1, H // 4, W // 4)
+    d0, d1 = torch.from_numpy(f0).cuda(), torch.from_numpy(f1).cuda()
+    net.prepare(0, d0.data_ptr(), d1.data_ptr(), W, H, reduce=reduce)
+    out = torch.empty(1, h4, w4, 3, device="cuda")
+    dims = list(zip(net_oracle.CIN, net_oracle.COUT))
+    for c in range(16):
+        p = np.zeros(param_count(), np.float32)
+        k = 0
+        for l, (ci, co) in enumerate(dims):
+            Wl = np.zeros((co, 9, ci), np.float32)
+            if l == 0:
+                Wl[0, 4, c], Wl[1, 4, c], Wl[2, 4, 16 + c], Wl[3, 4, 16 + c] = 1, -1, 1, -1
+            elif l < 5:
+                for q in range(4):
+                    Wl[q, 4, q] = 1
+            else:
+                Wl[0, 4, 0], Wl[0, 4, 1], Wl[1, 4, 2], Wl[1, 4, 3] = 1, -1, 1, -1
+            p[k:k + co * 9 * ci] = Wl.ravel()
+            k += co * 9 * ci + co
+        net.set_params(p)
+        net.forward(1, h4, w4, out.data_ptr())
+        torch.cuda.synchronize()
+        o = out[0].cpu().numpy()
+        assert np.array_equal(o[..., 0], want[..., c]), (reduce, c)
+        assert np.array_equal(o[..., 1], want[..., 16 + c]), (reduce, c)
+    net.close()
+
+
+def test_input_reduction_rejected():
+    net = ProposalNet(1, 8, 8)
+    d = torch.zeros(32, 32, dtype=torch.uint8, device="cuda")
+    with pytest.raises(bm.BriefMatchException, match="reduce must be 1, 2 or 4"):
+        net.prepare(0, d.data_ptr(), d.data_ptr(), 32, 32, reduce=3)
+    with pytest.raises(bm.BriefMatchException, match="beyond the network's buffers"):
+        net.prepare(0, d.data_ptr(), d.data_ptr(), 12, 32, reduce=4)  # (12 / 4) / 4 = 0 cells
+    net.close()
 
 
 def test_tcgen05_path_is_the_default():

@@ -97,6 +97,13 @@ def test_seed_rejects_bad_arguments():
         bm.seed(eng, True, d.data_ptr(), 4, 4, 1.0)
     with pytest.raises(bm.BriefMatchException):
         bm.seed(eng, True, d.data_ptr(), 0, 4, 0.5)
+    with pytest.raises(bm.BriefMatchException, match="reduce must be 1, 2 or 4"):
+        bm.set_proposal_reduce(eng, 8)
+    small, _ = make_engine(small_params(40, 12))
+    bm.set_proposal_reduce(small, 2)
+    with pytest.raises(bm.BriefMatchException, match="frame too small"):
+        bm.set_proposal_reduce(small, 4)  # 12 rows < 4 * 4
+    small.clean()
 
 
 def _net_with_spread_logits(h4, w4, seed=3):
@@ -109,28 +116,41 @@ def _net_with_spread_logits(h4, w4, seed=3):
     return net
 
 
-@pytest.mark.parametrize("local", [(), (2, 1)])
-def test_seeded_sequence_matches_oracle(local):
+@pytest.mark.parametrize("local,reduce", [((), 1), ((2, 1), 1), ((), 2), ((2, 1), 4)])
+def test_seeded_sequence_matches_oracle(local, reduce):
+    """The seeded frame loop against the oracle's, with the network on the frames
+    (cells of 4 pixels) and on frames reduced 2x and 4x (cells of 8 and 16, bm_set_proposal_reduce)."""
     W, H = 88, 64
     prm = small_params(W, H, 2.0, 2.0, N=64)
     eng, pattern = make_engine(prm, pattern_seed=4)
-    h4, w4 = H // 4, W // 4
-    net = _net_with_spread_logits(h4, w4)
+    h4, w4 = H // reduce // 4, W // reduce // 4
+    net = _net_with_spread_logits(H // 4, W // 4)
     it, jf = 1, 8
     bm.set_proposal(eng, net, 0.5, it, jf)
+    if reduce != 1:
+        bm.set_proposal_reduce(eng, reduce)
     if local:
         bm.set_local_steps(eng, len(local), local[0])
 
-    def pred_fn(prev_u8, cur_u8):
+    def pred_fn(prev_u8, cur_u8, check=True):
         d0, d1 = _dev(prev_u8), _dev(cur_u8)
         out = torch.empty(h4, w4, 3, device="cuda")
         st = torch.cuda.current_stream().cuda_stream
-        net.prepare(0, d0.data_ptr(), d1.data_ptr(), W, H, st)
+        net.prepare(0, d0.data_ptr(), d1.data_ptr(), W, H, st, reduce=reduce)
         net.forward(1, h4, w4, out.data_ptr(), st)
         torch.cuda.synchronize()
         o = out.cpu().numpy()
-        assert (o[..., 2] >= 0).any() and (o[..., 2] < 0).any()
+        if check:
+            assert (o[..., 2] >= 0).any() and (o[..., 2] < 0).any()
         return o
+
+    frames, _ = synth.make_sequence(8, W, H, 4, vmax=5.0)
+    # centre the confidence logits of the first pair on 0 (the head's logit bias is
+    # the last parameter), so that some cells are seeded and some are not even on the
+    # few cells of a 4x reduced input
+    p = net.params()
+    p[-1] -= float(np.median(pred_fn(frames[0], frames[1], check=False)[..., 2]))
+    net.set_params(p)
 
     normals_cache = {}
 
@@ -140,8 +160,7 @@ def test_seeded_sequence_matches_oracle(local):
         return normals_cache[call]
 
     seq = oracle.Sequence(prm.as_dict(), pattern, normals_fn, nn=eng.nn_indices(),
-                          proposal=(pred_fn, 0.0, it, jf, local))
-    frames, _ = synth.make_sequence(8, W, H, 4, vmax=5.0)
+                          proposal=(pred_fn, 0.0, it, jf, local, reduce))
     for k, f in enumerate(frames):
         d = _dev(f)
         u = torch.empty(H, W, device="cuda")
@@ -179,9 +198,10 @@ def test_detached_proposal_is_plain():
     assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
 
 
-def test_batch_seeded_equals_single_contexts():
+@pytest.mark.parametrize("reduce", [1, 2])
+def test_batch_seeded_equals_single_contexts(reduce):
     """A batch with a proposal attached gives, for every pair of uneven size, what a
-    fresh context with the same proposal attached gives."""
+    fresh context with the same proposal (and input reduction) attached gives."""
     sizes = [(96, 64), (120, 72), (72, 56)]
     params = [small_params(w, h, 2.0, 2.0, N=64) for w, h in sizes]
     frames = [synth.make_pair(60 + k, w, h, 5.0)[:2] for k, (w, h) in enumerate(sizes)]
@@ -190,11 +210,13 @@ def test_batch_seeded_equals_single_contexts():
     for p, (f0, f1) in zip(params, frames):
         eng = bm.FlowEngine(p)
         bm.set_proposal(eng, net, 0.5, 1, 8)
+        bm.set_proposal_reduce(eng, reduce)
         eng.process_frame(f0)
         want.append(eng.process_frame(f1))
         eng.clean()
     b = bm.Batch(params)
     b.set_proposal(net, 0.5, 1, 8)
+    b.set_proposal_reduce(reduce)
     b.set_local_steps(0, 1)
     with pytest.raises(bm.BriefMatchException):
         b.set_schedule(per_pair=0)
