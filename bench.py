@@ -636,7 +636,8 @@ def run_engine(args, torch, world, rank):
         "data": "synthetic (seeded generator; see bench.py)",
         "config": bench_config(world),
         "engine": {"name": head_name, "iterations": sched["iterations"], "jfMax": sched["jfMax"],
-                   "local_steps": sched.get("local_steps", 0), "grid": [prm.sx, prm.sy], "fsize": prm.fsize,
+                   "local_steps": sched.get("local_steps", 0), "proposal_reduce": sched.get("reduce"),
+                   "grid": [prm.sx, prm.sy], "fsize": prm.fsize,
                    "pipelined": PIPELINED},
         "plain": {"value": rp["value"], "ms_per_step": rp["ms_per_step"], "epe_mean": float(np.mean(rp["epe"])),
                   "gpu_launches": int(rp["launches"]), "iterations": prm.iterations, "jfMax": prm.jfMax},
