@@ -116,7 +116,7 @@ std::string format_frame(const std::string& pattern, unsigned int frame)
 OFPipeline::OFPipeline()
     : m_doWriteMOT(false), m_doWriteFLO(false), m_doWriteLDR(false), m_verbose(false), m_doPrintError(false),
       m_endFrame(0), m_frame(0), m_stepFrame(1), m_startFrame(0), m_sx(0), m_sy(0), m_sx_in(0), m_sy_in(0), m_c(0),
-      m_rng("xorwow"), m_seed(0), m_propIterations(1), m_propJfMax(128), m_propLocalSteps(2), m_net(nullptr), m_bm(nullptr),
+      m_rng("xorwow"), m_seed(0), m_propIterations(1), m_propJfMax(128), m_propLocalSteps(2), m_propReduce(1), m_net(nullptr), m_bm(nullptr),
       m_bmP(nullptr), m_first(true)
 {
 }
@@ -175,6 +175,8 @@ bool OFPipeline::setParams(int argc, char* argv[])
               10000u);
     args.uint(&m_propLocalSteps, "--proposal-local-steps", "-pls",
               "Local refinement steps (radius 2, then 1) after seeding by the proposal", 0u, 16u);
+    args.uint(&m_propReduce, "--proposal-reduce", "-prd",
+              "Proposal network on the frames reduced 1x, 2x or 4x (2 for frames much larger than 512x384)", 1u, 4u);
     if (!args.read(argc, argv)) return false;
     m_seed = seed;
     if (m_rng != "xorwow" && m_rng != "philox")
@@ -259,8 +261,10 @@ void OFPipeline::setup()
         bm_throw_on_error(bm_net_set_params(m_net, w.data(), w.size()));
         bm_throw_on_error(bm_set_proposal(m_bm->context(), m_net, 0.5f, m_propIterations, m_propJfMax));
         bm_throw_on_error(bm_set_local_steps(m_bm->context(), m_propLocalSteps, 2));
-        std::fprintf(stderr, "Proposal:                %s (%u iterations, jump-flooding max %u, %u local steps)\n\n",
-                     m_proposal.c_str(), m_propIterations, m_propJfMax, m_propLocalSteps);
+        bm_throw_on_error(bm_set_proposal_reduce(m_bm->context(), m_propReduce));
+        std::fprintf(stderr,
+                     "Proposal:                %s (%u iterations, jump-flooding max %u, %u local steps, input reduced %ux)\n\n",
+                     m_proposal.c_str(), m_propIterations, m_propJfMax, m_propLocalSteps, m_propReduce);
     }
     m_frameData.resize((size_t)m_sx_in * m_sy_in);
     m_first = true;

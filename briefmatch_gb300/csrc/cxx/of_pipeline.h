@@ -29,7 +29,7 @@ private:
     unsigned int m_endFrame, m_frame, m_stepFrame, m_startFrame, m_sx, m_sy, m_sx_in, m_sy_in, m_c;
     std::string m_input, m_flowGT, m_output, m_rng, m_proposal;
     unsigned long long m_seed;
-    unsigned int m_propIterations, m_propJfMax, m_propLocalSteps;
+    unsigned int m_propIterations, m_propJfMax, m_propLocalSteps, m_propReduce;
     bm_net* m_net;
     BriefMatch* m_bm;
     BMParams* m_bmP;

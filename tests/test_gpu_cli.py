@@ -71,8 +71,10 @@ def test_cli_bin_png_and_epe(tmp_path):
         assert np.array_equal(rgb, oracle.flow_colors(fu, fv, mm)), mm
 
 
-def test_cli_proposal_matches_library(tmp_path):
-    """--proposal seeds every pair with the learned proposal, as bm_set_proposal does."""
+@pytest.mark.parametrize("reduce", [1, 2])
+def test_cli_proposal_matches_library(tmp_path, reduce):
+    """--proposal seeds every pair with the learned proposal, as bm_set_proposal does
+    (--proposal-reduce as bm_set_proposal_reduce)."""
     from briefmatch_gb300 import learn
 
     W, H = 120, 80
@@ -80,12 +82,14 @@ def test_cli_proposal_matches_library(tmp_path):
     for k, f in enumerate(frames):
         write_pgm(str(tmp_path / ("f%02d.pgm" % k)), f)
     run("-i", str(tmp_path / "f%02d.pgm"), "-f", "0:2", "-o", str(tmp_path / "o%02d.flo"), "-ux", "2", "-uy", "2",
-        "-fl", "64", "--proposal", learn.DEFAULT_WEIGHTS, "-pit", "1", "-pjm", "8", "-pls", "2")
+        "-fl", "64", "--proposal", learn.DEFAULT_WEIGHTS, "-pit", "1", "-pjm", "8", "-pls", "2",
+        "--proposal-reduce", str(reduce))
     prm = bm.BMParams.derive(W, H, 2.0, 2.0, N=64)
     eng = bm.FlowEngine(prm)
     net = learn.load_net(learn.DEFAULT_WEIGHTS, 1, H // 4, W // 4)
     bm.set_proposal(eng, net, 0.5, 1, 8)
     bm.set_local_steps(eng, 2, 2)
+    bm.set_proposal_reduce(eng, reduce)
     for k, f in enumerate(frames):
         u, v = eng.process_frame(f)
         fu, fv = read_flo(str(tmp_path / ("o%02d.flo" % k)))
