@@ -1059,6 +1059,11 @@ struct bm_net {
     float* d_loss = nullptr;            // 3 floats
     uint64_t step = 0;
     bool packed = false;
+    // bm_net_snapshot: two slots, each a device copy of the master parameters and both
+    // Adam moments (3 * nparam floats, allocated on first use) and the step count
+    float* d_snap = nullptr;
+    uint64_t snap_step[2] = {};
+    bool has_snap[2] = {};
 
     // tcgen05 path (k_conv_umma): tensor maps of the weights (fixed buffers) and of the
     // activations for the last (B, h, w) seen; error word of its bounded waits
@@ -1278,7 +1283,7 @@ bm_status bm_net_destroy(bm_net* n)
 {
     if (!n) return BM_OK;
     void* ptrs[] = {n->d_master, n->d_grad, n->d_m, n->d_v, n->d_in, n->d_out, n->d_loss, n->d_dy[0], n->d_dy[1],
-                    n->d_err, n->d_bar};
+                    n->d_err, n->d_bar, n->d_snap};
     for (void* q : ptrs)
         if (q) bmk::device_free(q);
     for (int l = 0; l < NL; l++) {
@@ -1306,6 +1311,43 @@ bm_status bm_net_get_params(bm_net* n, float* h_params, size_t count)
 {
     if (!n || !h_params || count != n->nparam) return nfail(BM_ERR_INVALID, "bm_net_get_params: wrong parameter count");
     BN_CUDA(cudaMemcpy(h_params, n->d_master, count * 4, cudaMemcpyDeviceToHost));
+    return BM_OK;
+}
+
+// Training state (master parameters, Adam moments, step count) copied into snapshot
+// slot 0 or 1 on `stream`, and copied back by bm_net_restore: a training loop rolls
+// back to a validated snapshot when the loss spikes instead of continuing from a
+// collapsed network.
+bm_status bm_net_snapshot(bm_net* n, uint32_t slot, void* stream)
+{
+    if (!n || slot > 1) return nfail(BM_ERR_INVALID, "bm_net_snapshot: null network or slot not 0 or 1");
+    const size_t np = n->nparam;
+    if (!n->d_snap && bmk::device_malloc((void**)&n->d_snap, 6 * np * sizeof(float)) != cudaSuccess) {
+        n->d_snap = nullptr;
+        return nfail(BM_ERR_NOMEM, "bm_net_snapshot: allocation failed");
+    }
+    float* dst = n->d_snap + 3 * np * slot;
+    cudaStream_t st = (cudaStream_t)stream;
+    BN_CUDA(cudaMemcpyAsync(dst, n->d_master, np * 4, cudaMemcpyDeviceToDevice, st));
+    BN_CUDA(cudaMemcpyAsync(dst + np, n->d_m, np * 4, cudaMemcpyDeviceToDevice, st));
+    BN_CUDA(cudaMemcpyAsync(dst + 2 * np, n->d_v, np * 4, cudaMemcpyDeviceToDevice, st));
+    n->snap_step[slot] = n->step;
+    n->has_snap[slot] = true;
+    return BM_OK;
+}
+
+bm_status bm_net_restore(bm_net* n, uint32_t slot, void* stream)
+{
+    if (!n || slot > 1) return nfail(BM_ERR_INVALID, "bm_net_restore: null network or slot not 0 or 1");
+    if (!n->has_snap[slot]) return nfail(BM_ERR_STATE, "bm_net_restore: no snapshot in this slot");
+    const size_t np = n->nparam;
+    const float* src = n->d_snap + 3 * np * slot;
+    cudaStream_t st = (cudaStream_t)stream;
+    BN_CUDA(cudaMemcpyAsync(n->d_master, src, np * 4, cudaMemcpyDeviceToDevice, st));
+    BN_CUDA(cudaMemcpyAsync(n->d_m, src + np, np * 4, cudaMemcpyDeviceToDevice, st));
+    BN_CUDA(cudaMemcpyAsync(n->d_v, src + 2 * np, np * 4, cudaMemcpyDeviceToDevice, st));
+    n->step = n->snap_step[slot];
+    n->packed = false;   // the BF16 layouts are rebuilt from the restored parameters
     return BM_OK;
 }
 

@@ -158,10 +158,56 @@ def build_set(torch, n, target_iterations, chunk=256, workers=None, kind="sequen
     return f0, f1, tgt, gt
 
 
-def train_net(torch, net, f0, f1, tgt, idx_train, epochs, batch, lr, seed=1, log=print):
+SPIKE_FACTOR = 8.0     # a flow loss this many times the recent median is a spike
+SPIKE_WINDOW = 200     # steps in that median
+SNAPSHOT_EVERY = 500   # steps between snapshots of the training state
+
+
+class SpikeGuard:
+    """Loss-spike rollback of a training loop over a ProposalNet (bm_net_snapshot /
+    bm_net_restore; host bookkeeping only).  Every `every` steps the training state
+    goes into the snapshot slot that does not hold the newest validated snapshot; a
+    snapshot counts as validated once the next step's loss, computed with it, is
+    steady.  A step whose flow loss exceeds `factor` times the median of the last
+    `window` steady steps restores the newest validated snapshot."""
+
+    def __init__(self, net, stream=0, factor=SPIKE_FACTOR, window=SPIKE_WINDOW, every=SNAPSHOT_EVERY):
+        from collections import deque
+
+        self.net, self.stream, self.factor, self.every = net, stream, factor, every
+        self.recent = deque(maxlen=window)
+        self.good = None      # slot of the newest validated snapshot
+        self.pending = None   # slot written after the previous step, validated by this one
+        self.rollbacks = 0
+
+    def step(self, step, flow):
+        """Account for the loss of training step `step` (1-based); True when the step
+        was a spike and the network went back to a validated snapshot (or, before the
+        first one, when the step is only left out of the median)."""
+        full = len(self.recent) == self.recent.maxlen
+        if full and flow > self.factor * float(np.median(self.recent)):
+            self.pending = None
+            if self.good is not None:
+                self.net.restore(self.good, self.stream)
+                self.rollbacks += 1
+            return True
+        self.recent.append(flow)
+        if self.pending is not None:
+            self.good, self.pending = self.pending, None
+        if len(self.recent) == self.recent.maxlen and (self.good is None or step % self.every == 0):
+            self.pending = 0 if self.good is None else self.good ^ 1
+            self.net.snapshot(self.pending, self.stream)
+        return False
+
+
+def train_net(torch, net, f0, f1, tgt, idx_train, epochs, batch, lr, seed=1, log=print, rollback=True):
     """Adam with cosine decay over `epochs` passes of idx_train; every step runs the
-    engine's kernels (input preparation, forward, backward, Adam).  Returns the
-    loss history [(step, flow loss, confidence loss)]."""
+    engine's kernels (input preparation, forward, backward, Adam).  With `rollback` a
+    SpikeGuard returns the network to a validated snapshot after a loss spike and
+    training goes on with the next batches: an unclipped update can otherwise leave
+    the network dead for the rest of the run.  Returns the loss history [(step, flow
+    loss, confidence loss)]; a rollback appears as an entry with the flow loss
+    negated."""
     h4, w4 = TRAIN_H // 4, TRAIN_W // 4
     stream = torch.cuda.current_stream().cuda_stream
     d_bt = torch.empty(batch, h4, w4, 3, device="cuda")
@@ -170,6 +216,7 @@ def train_net(torch, net, f0, f1, tgt, idx_train, epochs, batch, lr, seed=1, log
     total = max(1, steps_per_epoch * epochs)
     step = 0
     hist = []
+    guard = SpikeGuard(net, stream) if rollback else None
     for ep in range(epochs):
         order = rng.permutation(idx_train)
         for k in range(steps_per_epoch):
@@ -180,6 +227,11 @@ def train_net(torch, net, f0, f1, tgt, idx_train, epochs, batch, lr, seed=1, log
             cur = lr * 0.5 * (1 + np.cos(np.pi * step / total))
             loss = net.train_step(batch, h4, w4, d_bt.data_ptr(), float(cur), 0, stream)
             step += 1
+            if guard is not None and guard.step(step, float(loss[0])):
+                hist.append((step, -float(loss[0]), float(loss[1])))
+                if log:
+                    log("step %d/%d  flow loss %.4f: spike, back to the last validated snapshot" % (step, total, loss[0]))
+                continue
             if step % 50 == 0 or step == total or step == 1:
                 hist.append((step, float(loss[0]), float(loss[1])))
                 if log:

@@ -37,6 +37,8 @@ def _declare():
         "bm_net_set_umma": (c.c_int, [c.c_void_p, c.c_int]),
         "bm_net_umma": (c.c_int, [c.c_void_p]),
         "bm_net_check": (c.c_int, [c.c_void_p, c.c_void_p]),
+        "bm_net_snapshot": (c.c_int, [c.c_void_p, c.c_uint32, c.c_void_p]),
+        "bm_net_restore": (c.c_int, [c.c_void_p, c.c_uint32, c.c_void_p]),
         "bm_net_fused_ctas": (c.c_int, [c.c_void_p]),
     }
     for name, (res, args) in sig.items():
@@ -128,6 +130,14 @@ class ProposalNet:
     def check(self, stream=0):
         """Raises if a tensor-core layer's bounded wait gave up (bm_net_check)."""
         check(lib().bm_net_check(self._n, ctypes.c_void_p(stream)))
+
+    def snapshot(self, slot=0, stream=0):
+        """Copy the training state into snapshot slot 0 or 1 (bm_net_snapshot)."""
+        check(lib().bm_net_snapshot(self._n, slot, ctypes.c_void_p(stream)))
+
+    def restore(self, slot=0, stream=0):
+        """Return to the training state of snapshot slot 0 or 1 (bm_net_restore)."""
+        check(lib().bm_net_restore(self._n, slot, ctypes.c_void_p(stream)))
 
     def train_step(self, B, h, w, d_target, lr, d_grad=0, stream=0):
         loss = np.zeros(3, np.float32)

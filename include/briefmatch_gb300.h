@@ -338,6 +338,14 @@ bm_status bm_net_forward(bm_net* n, uint32_t B, uint32_t h, uint32_t w, float* d
  * h_loss (may be NULL) receives (flow loss, confidence loss, confident fraction). */
 bm_status bm_net_train_step(bm_net* n, uint32_t B, uint32_t h, uint32_t w, const float* d_target, float lr,
                             float* d_grad_out, float* h_loss, void* stream);
+/* No counterpart in the reference.  Training state -- master parameters, both Adam
+ * moments and the step count -- copied into snapshot slot 0 or 1 on `stream` (device
+ * memory allocated on first use: BM_ERR_NOMEM if that fails), and copied back by
+ * bm_net_restore (BM_ERR_STATE for a slot never written).  A training loop rolls back
+ * to a snapshot that later steps validated when the loss spikes.  Synchronise
+ * `stream` before reading the parameters with bm_net_get_params. */
+bm_status bm_net_snapshot(bm_net* n, uint32_t slot, void* stream);
+bm_status bm_net_restore(bm_net* n, uint32_t slot, void* stream);
 /* Which tensor-core path the convolutions take.  mode 1 (the default where the driver
  * encodes tensor maps): every layer of the forward pass, and the backward-data pass of
  * the 32-channel layers, is a launch of tcgen05 MMAs into tensor memory fed by TMA;

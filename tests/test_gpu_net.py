@@ -132,6 +132,54 @@ def test_input_reduction_rejected():
     net.close()
 
 
+def test_snapshot_restore_returns_to_the_training_state():
+    """bm_net_snapshot / bm_net_restore: after Adam steps, restoring slot 0 gives back
+    the parameters and the forward output of the snapshot, and the Adam moments too
+    (the same steps from there reach the same parameters); slot 1 keeps its own state;
+    a slot never written is refused."""
+    B, h, w = 2, 12, 20
+    net, p0, x, tgt = _setup(B, h, w, seed=5)
+    d_t = torch.from_numpy(tgt).cuda()
+    out = torch.empty(B, h, w, 3, device="cuda")
+
+    def fwd():
+        net.forward(B, h, w, out.data_ptr())
+        torch.cuda.synchronize()
+        return out.cpu().numpy().copy()
+
+    def steps(k):
+        for _ in range(k):
+            net.train_step(B, h, w, d_t.data_ptr(), 1e-2)
+        torch.cuda.synchronize()
+
+    with pytest.raises(bm.BriefMatchException, match="no snapshot"):
+        net.restore(0)
+    with pytest.raises(bm.BriefMatchException, match="slot not 0 or 1"):
+        net.snapshot(2)
+    steps(2)
+    net.snapshot(0)
+    torch.cuda.synchronize()
+    pa, oa = net.params(), fwd()
+    steps(3)
+    pb = net.params()
+    assert not np.array_equal(pa, pb)
+    net.snapshot(1)
+    net.restore(0)
+    torch.cuda.synchronize()
+    assert np.array_equal(net.params(), pa) and np.array_equal(fwd(), oa)
+    steps(3)
+    # FP32 atomics in the weight gradients may sum in another order, which can flip
+    # the sign of Adam's step for a parameter whose gradient is near zero: all but a
+    # handful of parameters replay the same steps
+    pr = net.params()
+    assert np.mean(np.abs(pr - pb) > 1e-5) < 1e-3, np.sort(np.abs(pr - pb))[-5:]
+    assert np.mean(np.abs(pr - pb)) < 1e-3 * np.mean(np.abs(pb - pa))
+    net.restore(1)
+    torch.cuda.synchronize()
+    assert np.array_equal(net.params(), pb)
+    net.close()
+
+
 def test_tcgen05_path_is_the_default():
     net = ProposalNet(1, 8, 8)
     assert net.umma == 1

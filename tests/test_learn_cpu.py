@@ -38,3 +38,64 @@ def test_crops_are_windows_of_an_uneven_pair():
 def test_unknown_kind_rejected():
     with pytest.raises(ValueError):
         learn._group(0, "frames")
+
+
+class _FakeNet:
+    """Records the snapshot/restore calls of a SpikeGuard; the 'state' is the step at
+    which each slot was written."""
+
+    def __init__(self):
+        self.slots = {}
+        self.calls = []
+        self.now = 0
+
+    def snapshot(self, slot, stream=0):
+        self.slots[slot] = self.now
+        self.calls.append(("snapshot", slot, self.now))
+
+    def restore(self, slot, stream=0):
+        assert slot in self.slots
+        self.calls.append(("restore", slot, self.slots[slot]))
+
+
+def _drive(guard, net, losses):
+    rolled = []
+    for step, flow in enumerate(losses, start=1):
+        net.now = step
+        if guard.step(step, flow):
+            rolled.append(step)
+    return rolled
+
+
+def test_spike_guard_restores_the_newest_validated_snapshot():
+    net = _FakeNet()
+    g = learn.SpikeGuard(net, factor=8.0, window=20, every=50)
+    losses = [0.02] * 120
+    losses[74] = 1.0    # step 75: a spike between snapshots
+    losses[100] = 1.0   # step 101: a spike right after the step-100 snapshot, before it is validated
+    rolled = _drive(g, net, losses)
+    assert rolled == [75, 101]
+    snaps = [c for c in net.calls if c[0] == "snapshot"]
+    restores = [c for c in net.calls if c[0] == "restore"]
+    # the first snapshot once the window is full (step 20), then every 50 steps
+    assert [c[2] for c in snaps] == [20, 50, 100]
+    # step 75 goes back to the step-50 snapshot (validated at 51); step 101 cannot use
+    # the unvalidated step-100 snapshot and goes back to the step-50 one again
+    assert [c[2] for c in restores] == [50, 50]
+    # the validated slot is never overwritten
+    assert snaps[1][1] != snaps[0][1] and snaps[2][1] != snaps[1][1]
+    assert g.rollbacks == 2
+
+
+def test_spike_guard_without_a_snapshot_only_skips():
+    net = _FakeNet()
+    g = learn.SpikeGuard(net, factor=8.0, window=10, every=100)
+    losses = [0.5] * 10 + [5.0] + [0.5] * 3
+    rolled = _drive(g, net, losses)
+    # step 10 fills the window and writes the first snapshot; step 11 spikes before it
+    # is validated: nothing to restore, the step is only left out
+    assert rolled == [11]
+    assert not [c for c in net.calls if c[0] == "restore"]
+    assert g.rollbacks == 0
+    # the next steady step writes a fresh snapshot
+    assert [c[2] for c in net.calls if c[0] == "snapshot"] == [10, 12]
