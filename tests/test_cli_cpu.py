@@ -34,6 +34,16 @@ def test_help_lists_every_reference_option():
         assert opt in out
 
 
+def test_help_lists_the_engine_options():
+    """Options the engine adds to the reference's: random stream, pattern seed, and the
+    learned proposal with its schedule and input reduction."""
+    rc, out, _ = run("-h")
+    assert rc == 1
+    for opt in ("--random-stream", "--pattern-seed", "--proposal", "--proposal-iterations", "--proposal-jf-max",
+                "--proposal-local-steps", "--proposal-reduce"):
+        assert opt in out
+
+
 @pytest.mark.parametrize("args,msg", [
     ((), "Missing required option '--input'"),
     (("-i", "x.pgm", "-fl", "600"), "Valid range is [2, 512]"),
@@ -44,6 +54,7 @@ def test_help_lists_every_reference_option():
     (("-i", "x.pgm", "-f", "3"), "Unable to parse frame range"),
     (("-i", "x.pgm", "-f", "5:2"), "End frame should be >= start frame"),
     (("-i", "x.pgm", "-rng", "mt"), "not valid"),
+    (("-i", "x.pgm", "--proposal-reduce", "8"), "out of range"),
 ])
 def test_parser_errors(args, msg):
     rc, _, err = run(*args)
